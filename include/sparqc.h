@@ -1,0 +1,181 @@
+/*
+ * sparqc.h -- C ABI of the GB300 sparse statevector gate engine.
+ *
+ * The state is a GPU open-addressing hash table mapping 64-bit basis-state keys to complex
+ * amplitudes. Gates are applied by pairing each key with k ^ (1 << target), updating the
+ * pair with its 2x2 matrix, writing the results into a fresh table and pruning negligible
+ * amplitudes after branching gates. All entry points take plain pointers and sizes, return
+ * an int status (SQC_OK = 0) and never throw.
+ *
+ * Reference interface replaced (ivanNovikau/SparQC, header-only C++, no C ABI of its own):
+ *   Circuit__(nq, hash_table_parameters)      emulator/include/circuit.h:34-43
+ *   x/y/z/h(t), phase/rz/rx/ry(t, par)         emulator/include/circuit.h:45-83
+ *   TableManager__::gate_sq / gate_sq_par      emulator/device/table_manager.cuh:311-340
+ *   set_zero_quantum_state                     emulator/device/table_manager.cuh:299-308
+ *   get_statevector (readout)                  emulator/device/table_manager.cuh:343-350,
+ *                                              emulator/device/table.cuh:47-75
+ *   hash_table_parameters                      emulator/include/sim_parameters_types.h:133-145
+ * The C++ drop-in class with the reference's names is in sparqc_circuit.hpp.
+ *
+ * Threading: a handle is bound to one CUDA stream and is not thread-safe; separate handles
+ * may be used from separate threads. Gate calls are asynchronous and may be buffered so
+ * that consecutive gates are fused into one device pass; sqc_sync, readout, nnz and norm
+ * queries flush and wait.
+ */
+#ifndef SPARQC_H
+#define SPARQC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+enum {
+    SQC_OK = 0,
+    SQC_ERR_ARG = 1,        /* bad argument (qubit out of range, target among controls, ...) */
+    SQC_ERR_OOM = 2,        /* device allocation failed */
+    SQC_ERR_TABLE_FULL = 3, /* probe limit reached and the table could not grow */
+    SQC_ERR_CUDA = 4,       /* CUDA runtime error (message in sqc_last_error) */
+    SQC_ERR_BUDGET = 5,     /* table memory would exceed the HBM budget */
+    SQC_ERR_CAPACITY = 6,   /* caller buffer too small (required size returned) */
+    SQC_ERR_NO_DEVICE = 7,  /* no CUDA device, or more devices requested than present */
+    SQC_ERR_STATE = 8       /* handle in an unusable state */
+};
+
+/* ---- gates --------------------------------------------------------------------------- */
+/* Kinds 0-7 are the reference's gates with the reference's argument meaning:
+ * phase(t, par) multiplies the bit-1 amplitude by e^{i par}; rz/rx/ry(t, par) rotate by par
+ * (cos/sin of par/2 are applied, emulator/device/table_manager.cuh:333-336).
+ * Kinds 8-12 are additions: S, Sdg (exact +-i on the bit-1 amplitude), T, Tdg (Phase with
+ * cos = +-sin = sqrt(1/2)) and U(theta, phi, lambda), the u3 matrix
+ * [[cos(theta/2), -e^{i lambda} sin(theta/2)], [e^{i phi} sin(theta/2), e^{i(phi+lambda)} cos(theta/2)]]. */
+enum {
+    SQC_X = 0, SQC_Y = 1, SQC_Z = 2, SQC_H = 3,
+    SQC_PHASE = 4, SQC_RZ = 5, SQC_RX = 6, SQC_RY = 7,
+    SQC_S = 8, SQC_SDG = 9, SQC_T = 10, SQC_TDG = 11, SQC_U = 12
+};
+
+typedef struct sqc_gate {
+    uint32_t kind;      /* SQC_X ... SQC_U */
+    uint32_t target;    /* target qubit: bit `target` of the key, qubit 0 = least significant */
+    uint64_t controls;  /* control mask: the gate acts on a key iff (key & controls) == controls */
+    double theta;       /* angle for phase/rz/rx/ry/u */
+    double phi;         /* u only */
+    double lambda;      /* u only */
+} sqc_gate;             /* 40 bytes */
+
+/* ---- construction -------------------------------------------------------------------- */
+/* Mirrors hash_table_parameters (emulator/include/sim_parameters_types.h:133-145).
+ * N_devices must be 1 (one GPU per state). coef_gpu_memory_reserve is the fraction of the
+ * device memory left free: tables may use at most (1 - reserve) * total memory.
+ * N_subtables and log2_N_bucket_spots are accepted for compatibility and ignored: buckets
+ * here always hold 16 keys (128 bytes of keys). */
+typedef struct sqc_hash_table_parameters {
+    uint32_t N_devices;
+    double coef_gpu_memory_reserve;
+    uint32_t N_subtables;
+    uint32_t log2_N_bucket_spots;
+} sqc_hash_table_parameters;
+
+enum { SQC_FP64 = 64, SQC_FP32 = 32 };
+
+typedef struct sqc_options {
+    uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 amplitudes */
+    double prune_threshold;    /* default 1e-14: prune iff |re| < thr && |im| < thr (in FP64) */
+    double load_factor;        /* target groups per bucket after growth, default 0.5 */
+    uint64_t initial_buckets;  /* initial bucket count (rounded to a power of two), 0 = 1024 */
+    void* stream;              /* cudaStream_t to run on; NULL = the handle creates its own */
+    uint32_t device;           /* CUDA device ordinal, default 0 */
+    uint32_t max_fused_gates;  /* cap on gates fused into one pass, 0 = default (64) */
+    uint32_t reserved[4];
+} sqc_options;
+
+typedef struct sqc_state sqc_state;
+
+/* Fill *opt with the defaults. */
+void sqc_default_options(sqc_options* opt);
+
+/* Create a state of nq qubits (1..64) set to |0...0>. params may be NULL (defaults), opt may
+ * be NULL (defaults). Replaces Circuit__::Circuit__ + TableManager__ construction. */
+int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt,
+               sqc_state** out);
+int sqc_destroy(sqc_state* st);
+
+/* |0...0>: key 0 with amplitude 1. Replaces TableManager__::set_zero_quantum_state. */
+int sqc_set_zero_state(sqc_state* st);
+
+/* Load n distinct (key, re, im) entries from host memory (amplitudes rounded to the state's
+ * precision). Keys must fit in nq bits. */
+int sqc_set_state(sqc_state* st, const uint64_t* keys, const double* re, const double* im,
+                  uint64_t n);
+
+/* ---- gates --------------------------------------------------------------------------- */
+/* Queue n gates (host array). Asynchronous. Replaces TableManager__::gate_sq/gate_sq_par. */
+int sqc_apply_gates(sqc_state* st, const sqc_gate* gates, uint64_t n);
+
+/* One-gate conveniences with the reference's names (emulator/include/circuit.h:45-83),
+ * uncontrolled. */
+int sqc_x(sqc_state* st, uint32_t t);
+int sqc_y(sqc_state* st, uint32_t t);
+int sqc_z(sqc_state* st, uint32_t t);
+int sqc_h(sqc_state* st, uint32_t t);
+int sqc_phase(sqc_state* st, uint32_t t, double par);
+int sqc_rz(sqc_state* st, uint32_t t, double par);
+int sqc_rx(sqc_state* st, uint32_t t, double par);
+int sqc_ry(sqc_state* st, uint32_t t, double par);
+
+/* Launch everything queued without waiting (the work is ordered on the handle's stream). */
+int sqc_flush(sqc_state* st);
+
+/* Launch everything queued, wait for it, check the device status word, grow the tables and
+ * replay if a pass ran out of table space. */
+int sqc_sync(sqc_state* st);
+
+/* ---- readout ------------------------------------------------------------------------- */
+enum { SQC_READ_SORTED = 1, SQC_READ_DROP_NEGLIGIBLE = 2 };
+
+/* Number of keys held (present entries, including any kept negligible ones). */
+int sqc_nnz(sqc_state* st, uint64_t* nnz);
+
+/* Copy the state into caller arrays of capacity cap. flags: SQC_READ_SORTED orders by key;
+ * SQC_READ_DROP_NEGLIGIBLE drops |re|,|im| < threshold entries as the reference's readout
+ * does (emulator/device/table.cuh:47-75). *n receives the count; if it exceeds cap the call
+ * returns SQC_ERR_CAPACITY and copies nothing. */
+int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_t cap,
+                  uint64_t* n, uint32_t flags);
+
+/* Sum of |amplitude|^2, accumulated in FP64 on the device. */
+int sqc_norm2(sqc_state* st, double* norm2);
+
+/* Compare two states of equal qubit count on the device (FP64 accumulation):
+ * fidelity = |<b|a>|^2 / (<a|a><b|b>), max_abs_err = max over keys of |a_k - b_k|. */
+int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_err);
+
+/* ---- introspection ------------------------------------------------------------------- */
+typedef struct sqc_stats {
+    uint64_t gates_applied;    /* gates executed on the device */
+    uint64_t passes;           /* device gate passes executed */
+    uint64_t kernel_launches;  /* kernels launched by this handle */
+    uint64_t buckets;          /* current buckets per table */
+    uint64_t table_bytes;      /* device bytes held by both tables */
+    uint64_t replays;          /* passes re-run after table growth */
+    uint64_t amp_updates;      /* sum over gates of input nonzeros (only counted after sync) */
+    uint64_t alg_bytes;        /* algorithmic bytes of the passes: (nnz_in + nnz_out) * (8 + A) per
+                                  key-changing pass, nnz * (8 + 2A) per pass that keeps every key;
+                                  A = 16 (FP64) or 8 (FP32). Since the last reset, after sync. */
+} sqc_stats;
+
+int sqc_get_stats(sqc_state* st, sqc_stats* out);
+const char* sqc_status_string(int status);
+/* Message of the last error on this handle ("" if none). Valid until the next call. */
+const char* sqc_last_error(sqc_state* st);
+/* The cudaStream_t the handle runs on. */
+void* sqc_stream(sqc_state* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPARQC_H */

@@ -33,6 +33,8 @@ def lib():
         L.orc_apply.argtypes = [P, P, U64]
         L.orc_nnz.restype = U64
         L.orc_nnz.argtypes = [P]
+        L.orc_amp_updates.restype = U64
+        L.orc_amp_updates.argtypes = [P]
         L.orc_get_state.restype = ctypes.c_int64
         L.orc_get_state.argtypes = [P, P, P, P, U64, I]
         L.orc_norm2.restype = D
@@ -87,6 +89,10 @@ class SparseOracle:
     @property
     def nnz(self):
         return int(self._L.orc_nnz(self._h))
+
+    @property
+    def amp_updates(self):
+        return int(self._L.orc_amp_updates(self._h))
 
     def state(self, sorted=True):
         n = self.nnz

@@ -54,6 +54,7 @@ typedef struct {
     uint64_t icap;      /* index capacity (power of two) */
     uint64_t *idx;      /* position+1, 0 = empty */
     int nthreads;
+    uint64_t amp_updates;  /* sum over applied gates of the input key count */
 } orc_state;
 
 typedef struct { double c, s; double m[8]; } coef_t;
@@ -328,6 +329,7 @@ static int apply_one(orc_state* st, const orc_gate* g) {
 
 int orc_apply(orc_state* st, const orc_gate* gates, uint64_t ngates) {
     for (uint64_t g = 0; g < ngates; ++g) {
+        st->amp_updates += st->n;
         int rc = apply_one(st, &gates[g]);
         if (rc) return rc;
     }
@@ -335,6 +337,8 @@ int orc_apply(orc_state* st, const orc_gate* gates, uint64_t ngates) {
 }
 
 uint64_t orc_nnz(const orc_state* st) { return st->n; }
+
+uint64_t orc_amp_updates(const orc_state* st) { return st->amp_updates; }
 
 static int cmp_u64(const void* a, const void* b) {
     uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;

@@ -1,0 +1,151 @@
+// extern "C" entry points of include/sparqc.h. Every call returns a status code; no C++
+// exception crosses the boundary (the reference throws std::string on the host and exits on
+// CUDA errors, emulator/device/table_manager.cuh:175-259, emulator/third_party/helper_cuda.h).
+#include <new>
+#include <string>
+
+#include "../../include/sparqc.h"
+#include "sqc_engine.h"
+
+struct sqc_state {
+    sqc::Engine eng;
+};
+
+namespace {
+
+template <class F>
+int guarded(sqc_state* st, F&& f) {
+    if (!st) return SQC_ERR_ARG;
+    try {
+        return f(st->eng);
+    } catch (const std::bad_alloc&) {
+        st->eng.err = "host allocation failed";
+        return SQC_ERR_OOM;
+    } catch (...) {
+        st->eng.err = "unexpected host exception";
+        return SQC_ERR_STATE;
+    }
+}
+
+int one(sqc_state* st, uint32_t kind, uint32_t t, double par) {
+    sqc_gate g;
+    g.kind = kind;
+    g.target = t;
+    g.controls = 0;
+    g.theta = par;
+    g.phi = 0.0;
+    g.lambda = 0.0;
+    return guarded(st, [&](sqc::Engine& e) { return e.apply(&g, 1); });
+}
+
+}  // namespace
+
+extern "C" {
+
+void sqc_default_options(sqc_options* opt) {
+    if (!opt) return;
+    opt->precision = SQC_FP64;
+    opt->prune_threshold = 1e-14;
+    opt->load_factor = 0.5;
+    opt->initial_buckets = 0;
+    opt->stream = nullptr;
+    opt->device = 0;
+    opt->max_fused_gates = 0;
+    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
+}
+
+int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt, sqc_state** out) {
+    if (!out) return SQC_ERR_ARG;
+    *out = nullptr;
+    sqc_state* st = nullptr;
+    try {
+        st = new sqc_state();
+    } catch (...) {
+        return SQC_ERR_OOM;
+    }
+    int rc;
+    try {
+        rc = st->eng.init(nq, params, opt);
+    } catch (...) {
+        rc = SQC_ERR_OOM;
+    }
+    if (rc != SQC_OK) {
+        delete st;
+        return rc;
+    }
+    *out = st;
+    return SQC_OK;
+}
+
+int sqc_destroy(sqc_state* st) {
+    delete st;
+    return SQC_OK;
+}
+
+int sqc_set_zero_state(sqc_state* st) { return guarded(st, [](sqc::Engine& e) { return e.set_zero(); }); }
+
+int sqc_set_state(sqc_state* st, const uint64_t* keys, const double* re, const double* im, uint64_t n) {
+    return guarded(st, [&](sqc::Engine& e) { return e.set_state(keys, re, im, n); });
+}
+
+int sqc_apply_gates(sqc_state* st, const sqc_gate* gates, uint64_t n) {
+    return guarded(st, [&](sqc::Engine& e) { return e.apply(gates, n); });
+}
+
+int sqc_x(sqc_state* st, uint32_t t) { return one(st, SQC_X, t, 0.0); }
+int sqc_y(sqc_state* st, uint32_t t) { return one(st, SQC_Y, t, 0.0); }
+int sqc_z(sqc_state* st, uint32_t t) { return one(st, SQC_Z, t, 0.0); }
+int sqc_h(sqc_state* st, uint32_t t) { return one(st, SQC_H, t, 0.0); }
+int sqc_phase(sqc_state* st, uint32_t t, double par) { return one(st, SQC_PHASE, t, par); }
+int sqc_rz(sqc_state* st, uint32_t t, double par) { return one(st, SQC_RZ, t, par); }
+int sqc_rx(sqc_state* st, uint32_t t, double par) { return one(st, SQC_RX, t, par); }
+int sqc_ry(sqc_state* st, uint32_t t, double par) { return one(st, SQC_RY, t, par); }
+
+int sqc_flush(sqc_state* st) { return guarded(st, [](sqc::Engine& e) { return e.flush(); }); }
+
+int sqc_sync(sqc_state* st) { return guarded(st, [](sqc::Engine& e) { return e.sync(); }); }
+
+int sqc_nnz(sqc_state* st, uint64_t* nnz) {
+    if (!nnz) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) { return e.nnz(nnz); });
+}
+
+int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
+    return guarded(st, [&](sqc::Engine& e) { return e.get_state(keys, re, im, cap, n, flags); });
+}
+
+int sqc_norm2(sqc_state* st, double* norm2) {
+    if (!norm2) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) { return e.norm2(norm2); });
+}
+
+int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_err) {
+    if (!b || !fidelity || !max_abs_err) return SQC_ERR_ARG;
+    return guarded(a, [&](sqc::Engine& e) { return e.compare(b->eng, fidelity, max_abs_err); });
+}
+
+int sqc_get_stats(sqc_state* st, sqc_stats* out) {
+    if (!out) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) { return e.stats(out); });
+}
+
+const char* sqc_status_string(int status) {
+    switch (status) {
+    case SQC_OK: return "ok";
+    case SQC_ERR_ARG: return "bad argument";
+    case SQC_ERR_OOM: return "out of memory";
+    case SQC_ERR_TABLE_FULL: return "table full";
+    case SQC_ERR_CUDA: return "CUDA error";
+    case SQC_ERR_BUDGET: return "HBM budget exceeded";
+    case SQC_ERR_CAPACITY: return "output capacity too small";
+    case SQC_ERR_NO_DEVICE: return "no suitable CUDA device";
+    case SQC_ERR_STATE: return "handle in an unusable state";
+    default: return "unknown status";
+    }
+}
+
+const char* sqc_last_error(sqc_state* st) { return st ? st->eng.err.c_str() : "null handle"; }
+
+void* sqc_stream(sqc_state* st) { return st ? (void*)st->eng.stream() : nullptr; }
+
+}  // extern "C"

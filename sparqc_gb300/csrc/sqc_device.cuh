@@ -1,0 +1,250 @@
+// Device-side layout and arithmetic of the sparse statevector table.
+//
+// Table layout (one table; a state owns two, used alternately as input and output):
+//   hdr [nb]          16-byte bucket headers {group, epoch, aux}
+//   keys[nb * 16]     64-bit keys, 16 per bucket (128 bytes)
+//   amps[nb * 16]     amplitudes, double2 (FP64) or float2 (FP32), same slot order
+// A bucket holds the keys of one group G = key >> 4 at slot key & 15. Buckets are found by
+// linear probing from mix(G) & (nb - 1). A bucket is live iff hdr.epoch equals the table's
+// current epoch (kept in the device control block), so a table never needs clearing: every
+// pass writes its output with a fresh epoch and stale headers read as empty. A slot is
+// occupied iff the low 4 bits of its stored key equal the slot index; empty slots hold
+// EMPTY(j) = 0xFFFF...F0 | (15 - j), whose low bits never equal j.
+//
+// The reference keeps one dense slot per basis state (identity hash, 2^nq slots,
+// emulator/device/table_manager.cuh:114-119, emulator/include/sim_parameters_types.h:153-158);
+// here the table is sized by load factor and holds only present keys, so 64-qubit keys work.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "sqc_types.h"
+
+namespace sqc {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27; x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31; return x;
+}
+
+__device__ __forceinline__ unsigned long long empty_key(int j) {
+    return 0xFFFFFFFFFFFFFFF0ULL | (unsigned long long)(15 - j);
+}
+
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+    unsigned lo = __shfl_sync(kFull, (unsigned)v, src);
+    unsigned hi = __shfl_sync(kFull, (unsigned)(v >> 32), src);
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+__device__ __forceinline__ Header load_hdr_cg(const Header* p) {
+    ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+    Header h;
+    h.group = v.x;
+    h.epoch = (unsigned)v.y;
+    h.aux = (unsigned)(v.y >> 32);
+    return h;
+}
+
+__device__ __forceinline__ Header load_hdr(const Header* p) {
+    ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
+    Header h;
+    h.group = v.x;
+    h.epoch = (unsigned)v.y;
+    h.aux = (unsigned)(v.y >> 32);
+    return h;
+}
+
+// 128-bit compare-and-swap on a bucket header. Returns the previous content.
+__device__ __forceinline__ Header cas_hdr(Header* p, const Header& expect, const Header& desired) {
+    unsigned long long e0 = expect.group, e1 = (unsigned long long)expect.epoch | ((unsigned long long)expect.aux << 32);
+    unsigned long long d0 = desired.group, d1 = (unsigned long long)desired.epoch | ((unsigned long long)desired.aux << 32);
+    unsigned long long o0, o1;
+    asm volatile(
+        "{\n\t.reg .b128 d, c, s;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 s, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], c, s;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(o0), "=l"(o1)
+        : "l"(e0), "l"(e1), "l"(d0), "l"(d1), "l"(p)
+        : "memory");
+    Header o;
+    o.group = o0;
+    o.epoch = (unsigned)o1;
+    o.aux = (unsigned)(o1 >> 32);
+    return o;
+}
+
+// Find the bucket of group G in a table that no one writes during the call. -1 if absent.
+__device__ __forceinline__ long long lookup_group(const TableDev& t, unsigned ep, unsigned long long G) {
+    unsigned long long b = mix64(G) & t.mask;
+    for (uint32_t i = 0; i < kMaxProbe; ++i) {
+        Header h = load_hdr(t.hdr + b);
+        if (h.epoch != ep) return -1;
+        if (h.group == G) return (long long)b;
+        b = (b + 1) & t.mask;
+    }
+    return -1;
+}
+
+// Claim (or find) the bucket of group G in a table being written with epoch ep. Linear
+// probing with a 128-bit CAS per attempt; bounded. -1 and ST_TABLE_FULL when no bucket
+// within kMaxProbe of the home bucket is free.
+__device__ __forceinline__ long long claim_group(const TableDev& t, unsigned ep, unsigned long long G,
+                                                 unsigned int* status) {
+    unsigned long long b = mix64(G) & t.mask;
+    Header cur = load_hdr_cg(t.hdr + b);
+    uint32_t probes = 0, attempts = 0;
+    while (probes < kMaxProbe && attempts < 4 * kMaxProbe) {
+        ++attempts;
+        if (cur.epoch == ep) {
+            if (cur.group == G) return (long long)b;
+            b = (b + 1) & t.mask;
+            ++probes;
+            cur = load_hdr_cg(t.hdr + b);
+            continue;
+        }
+        Header want;
+        want.group = G; want.epoch = ep; want.aux = 0;
+        Header old = cas_hdr(t.hdr + b, cur, want);
+        if (old.group == cur.group && old.epoch == cur.epoch && old.aux == cur.aux) return (long long)b;
+        cur = old;   // re-examine this bucket with its actual content
+    }
+    atomicCAS(status, 0u, (unsigned)ST_TABLE_FULL);
+    return -1;
+}
+
+// ---- arithmetic --------------------------------------------------------------------------
+// Explicit round-to-nearest operations: nothing is contracted, so every product and sum
+// rounds exactly as in the reference's source formulas (emulator/device/device_data.cuh:159-319).
+template <class T> struct Arith;
+template <> struct Arith<double> {
+    __device__ static __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    __device__ static __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    __device__ static __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    __device__ static __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+};
+template <> struct Arith<float> {
+    __device__ static __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    __device__ static __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    __device__ static __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    __device__ static __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+
+template <class T> struct Cx { T r, i; };
+
+// Sign flips and magnitude tests as integer operations: on this GPU every FP64 instruction,
+// compares and negations included, issues on the slow FP64 pipe. Both forms are exact.
+__device__ __forceinline__ double neg(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ float neg(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000u); }
+
+// Coefficients are read through a pointer to the (L1-cached, warp-broadcast) descriptor.
+template <class T> struct Coef;
+template <> struct Coef<double> {
+    __device__ static __forceinline__ double c(const GateDesc* g) { return __ldg(&g->c); }
+    __device__ static __forceinline__ double s(const GateDesc* g) { return __ldg(&g->s); }
+    __device__ static __forceinline__ double m(const GateDesc* g, int i) { return __ldg(&g->m[i]); }
+};
+template <> struct Coef<float> {
+    __device__ static __forceinline__ float c(const GateDesc* g) { return __ldg(&g->cf); }
+    __device__ static __forceinline__ float s(const GateDesc* g) { return __ldg(&g->sf); }
+    __device__ static __forceinline__ float m(const GateDesc* g, int i) { return __ldg(&g->mf[i]); }
+};
+
+template <class T>
+__device__ __forceinline__ Cx<T> cx_sel(bool p, Cx<T> a, Cx<T> b) { return p ? a : b; }
+
+// Branching update seen from one member of a pair: a = own amplitude, b = partner amplitude,
+// bit = own target bit. Each form below rounds exactly like the reference's pair formula for
+// that member (a + (-b) == a - b and (-s)*x == -(s*x) hold exactly in IEEE arithmetic):
+//   H : bit 0 -> f*(v0 + v1),             bit 1 -> f*(v0 - v1)
+//   Rx: c*own + s*(i-rotated partner)      (symmetric in the two members)
+//   Ry: bit 0 -> c*v0 - s*v1,             bit 1 -> c*v1 + s*v0
+//   U : self term first, then partner term, fused multiply-add chain (no reference form).
+template <class T>
+__device__ __forceinline__ Cx<T> branch_update(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
+    using A = Arith<T>;
+    Cx<T> o;
+    switch (kind) {
+    case KH: {
+        const T f = Coef<T>::c(g);
+        Cx<T> x = bit ? b : a;
+        Cx<T> y = bit ? Cx<T>{neg(a.r), neg(a.i)} : b;
+        o.r = A::mul(f, A::add(x.r, y.r));
+        o.i = A::mul(f, A::add(x.i, y.i));
+        break;
+    }
+    case KRX: {
+        const T c = Coef<T>::c(g), s = Coef<T>::s(g);
+        o.r = A::add(A::mul(c, a.r), A::mul(s, b.i));
+        o.i = A::sub(A::mul(c, a.i), A::mul(s, b.r));
+        break;
+    }
+    case KRY: {
+        const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
+        const T s = bit ? s0 : neg(s0);
+        o.r = A::add(A::mul(c, a.r), A::mul(s, b.r));
+        o.i = A::add(A::mul(c, a.i), A::mul(s, b.i));
+        break;
+    }
+    default: {  // KU
+        const T m00r = Coef<T>::m(g, 0), m00i = Coef<T>::m(g, 1), m01r = Coef<T>::m(g, 2), m01i = Coef<T>::m(g, 3);
+        const T m10r = Coef<T>::m(g, 4), m10i = Coef<T>::m(g, 5), m11r = Coef<T>::m(g, 6), m11i = Coef<T>::m(g, 7);
+        const T msr = bit ? m11r : m00r, msi = bit ? m11i : m00i;
+        const T mor = bit ? m10r : m01r, moi = bit ? m10i : m01i;
+        o.r = A::fma(neg(moi), b.i, A::fma(mor, b.r, A::fma(neg(msi), a.i, A::mul(msr, a.r))));
+        o.i = A::fma(moi, b.r, A::fma(mor, b.i, A::fma(msi, a.r, A::mul(msr, a.i))));
+        break;
+    }
+    }
+    return o;
+}
+
+// Diagonal update of one amplitude (reference: z_core, phase_core, rz_core).
+template <class T>
+__device__ __forceinline__ Cx<T> diag_update(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a) {
+    using A = Arith<T>;
+    switch (kind) {
+    case KZ: return bit ? Cx<T>{neg(a.r), neg(a.i)} : a;
+    case KS: return bit ? Cx<T>{neg(a.i), a.r} : a;
+    case KSDG: return bit ? Cx<T>{a.i, neg(a.r)} : a;
+    case KRZ: {
+        const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
+        const T s = bit ? s0 : neg(s0);   // bit 0: conj(a)*v0, bit 1: a*v1
+        return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
+    }
+    default: {  // KPHASE, KT, KTDG
+        if (!bit) return a;
+        const T c = Coef<T>::c(g), s = Coef<T>::s(g);
+        return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
+    }
+    }
+}
+
+// Swap update: the amplitude arriving from the partner (reference: x_core, y_core).
+template <class T>
+__device__ __forceinline__ Cx<T> swap_update(uint32_t kind, bool bit, Cx<T> b) {
+    if (kind == KX) return b;
+    return bit ? Cx<T>{neg(b.i), b.r} : Cx<T>{b.i, neg(b.r)};   // Y
+}
+
+__device__ __forceinline__ bool is_branch(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
+__device__ __forceinline__ bool is_swap(uint32_t k) { return k == KX || k == KY; }
+
+// Prune rule of the reference (emulator/include/data_t.h:50-60): |re| < thr && |im| < thr,
+// decided in FP64. For doubles |x| < thr is compared on the bit patterns (non-negative
+// doubles order like their bits; NaN compares false as in the FP64 test). For floats the
+// host passes the largest float f with (double)f < thr, so |x| <= f is the same FP64 test.
+__device__ __forceinline__ bool negligible(Cx<double> v, const PruneBits& t) {
+    const unsigned long long m = 0x7FFFFFFFFFFFFFFFULL;
+    return ((unsigned long long)__double_as_longlong(v.r) & m) < t.d &&
+           ((unsigned long long)__double_as_longlong(v.i) & m) < t.d;
+}
+__device__ __forceinline__ bool negligible(Cx<float> v, const PruneBits& t) {
+    return ((unsigned)__float_as_int(v.r) & 0x7FFFFFFFu) <= t.f && ((unsigned)__float_as_int(v.i) & 0x7FFFFFFFu) <= t.f;
+}
+
+}  // namespace sqc

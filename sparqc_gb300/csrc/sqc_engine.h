@@ -1,0 +1,102 @@
+// Host engine of one sparse state on one GPU: owns the two tables, the device control block,
+// the gate-descriptor buffer and the pass planner. Replaces the reference's TableManager__
+// (emulator/device/table_manager.cuh:45-353) and MappingFC__ launchers
+// (emulator/device/mapping_GHT.cuh:54-73).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/sparqc.h"
+#include "sqc_types.h"
+
+namespace sqc {
+
+struct HostTable {
+    Header* hdr = nullptr;
+    unsigned long long* keys = nullptr;
+    void* amps = nullptr;
+    unsigned long long nb = 0;
+};
+
+struct PassRec {
+    uint32_t first_gate;   // index into log_
+    uint32_t ngates;
+    int parity_in;
+    bool pair;
+};
+
+class Engine {
+public:
+    Engine() = default;
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    int init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt);
+    int set_zero();
+    int set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n);
+    int apply(const sqc_gate* gates, uint64_t n);
+    int sync();
+    int flush();
+    int nnz(uint64_t* out);
+    int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
+    int norm2(double* out);
+    int compare(Engine& b, double* fidelity, double* max_abs_err);
+    int stats(sqc_stats* out);
+    cudaStream_t stream() const { return stream_; }
+    uint32_t nq() const { return nq_; }
+
+    std::string err;
+
+private:
+    int fail(int code, const std::string& msg);
+    int cuda(cudaError_t e, const char* what);
+    size_t bucket_bytes() const;
+    int alloc_tables(unsigned long long nb, HostTable out[2]);
+    void free_tables(HostTable t[2]);
+    TableDev dev(const HostTable& t) const;
+    PassArgs pass_args() const;
+    int repair(size_t failed_pass);
+    int ensure_desc(size_t n);
+    int ensure_readout(size_t n);
+    GateDesc resolve(const sqc_gate& g) const;
+    bool streamable(const sqc_gate& g) const;
+    int read_ctl();
+
+    int device_ = 0;
+    int sms_ = 1;
+    uint32_t nq_ = 0;
+    bool dbl_ = true;
+    double thr_ = 1e-14;
+    double lf_ = 0.5;
+    uint32_t max_run_ = kMaxRun;
+    size_t budget_ = 0;
+    cudaStream_t stream_ = nullptr;
+    bool own_stream_ = false;
+
+    HostTable tab_[2];
+    Ctl* ctl_ = nullptr;        // device
+    Ctl* ctl_host_ = nullptr;   // pinned mirror
+    int parity_ = 0;            // table holding the state once every launched pass has run
+    unsigned long long seq_verified_ = 0;
+    PruneBits prune_{};
+
+    std::vector<sqc_gate> pending_;   // queued, not launched
+    std::vector<sqc_gate> log_;       // launched since the last verified sync
+    std::vector<PassRec> passes_;     // passes launched since the last verified sync
+
+    GateDesc* d_desc_ = nullptr;
+    GateDesc* h_desc_ = nullptr;
+    size_t desc_cap_ = 0, desc_used_ = 0;
+
+    unsigned long long* d_rk_ = nullptr;
+    double* d_rr_ = nullptr;
+    double* d_ri_ = nullptr;
+    size_t rcap_ = 0;
+
+    uint64_t gates_applied_ = 0, passes_run_ = 0, launches_ = 0, replays_ = 0;
+};
+
+}  // namespace sqc
