@@ -1,15 +1,16 @@
 // Device-side layout and arithmetic of the sparse statevector table.
 //
-// Table layout (one table; a state owns two, used alternately as input and output):
+// Table layout (one table per state, updated in place by every pass):
 //   hdr [nb]          16-byte bucket headers {group, epoch, aux}
-//   keys[nb * 16]     64-bit keys, 16 per bucket (128 bytes)
+//   keys[nb * 16]     64-bit stored keys, 16 per bucket (128 bytes)
 //   amps[nb * 16]     amplitudes, double2 (FP64) or float2 (FP32), same slot order
+//   list[nb]          indices of the live buckets, in claim order
 // A bucket holds the keys of one group G = key >> 4 at slot key & 15. Buckets are found by
-// linear probing from mix(G) & (nb - 1). A bucket is live iff hdr.epoch equals the table's
-// current epoch (kept in the device control block), so a table never needs clearing: every
-// pass writes its output with a fresh epoch and stale headers read as empty. A slot is
-// occupied iff the low 4 bits of its stored key equal the slot index; empty slots hold
-// EMPTY(j) = 0xFFFF...F0 | (15 - j), whose low bits never equal j.
+// linear probing from mix(G) & (nb - 1). A bucket is live iff hdr.epoch equals the state's
+// epoch, so a reset only bumps the epoch. A slot is occupied iff the low 4 bits of its
+// stored key equal the slot index; empty slots hold EMPTY(j) = 0xFFFF...F0 | (15 - j).
+// Live buckets are never freed between resets: a group whose keys are all pruned stays as an
+// empty live bucket, so probe chains never break.
 //
 // The reference keeps one dense slot per basis state (identity hash, 2^nq slots,
 // emulator/device/table_manager.cuh:114-119, emulator/include/sim_parameters_types.h:153-158);
@@ -37,8 +38,8 @@ __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int s
     return ((unsigned long long)hi << 32) | lo;
 }
 
-__device__ __forceinline__ Header load_hdr_cg(const Header* p) {
-    ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
+__device__ __forceinline__ Header load_hdr(const Header* p) {
+    ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
     Header h;
     h.group = v.x;
     h.epoch = (unsigned)v.y;
@@ -46,8 +47,8 @@ __device__ __forceinline__ Header load_hdr_cg(const Header* p) {
     return h;
 }
 
-__device__ __forceinline__ Header load_hdr(const Header* p) {
-    ulonglong2 v = *reinterpret_cast<const ulonglong2*>(p);
+__device__ __forceinline__ Header load_hdr_cg(const Header* p) {
+    ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2*>(p));
     Header h;
     h.group = v.x;
     h.epoch = (unsigned)v.y;
@@ -76,11 +77,12 @@ __device__ __forceinline__ Header cas_hdr(Header* p, const Header& expect, const
     return o;
 }
 
-// Find the bucket of group G in a table that no one writes during the call. -1 if absent.
+// Find the live bucket of group G, or -1. Correct while other threads claim buckets: a
+// claim only turns a non-live bucket live, and G's probe chain has no non-live bucket.
 __device__ __forceinline__ long long lookup_group(const TableDev& t, unsigned ep, unsigned long long G) {
     unsigned long long b = mix64(G) & t.mask;
     for (uint32_t i = 0; i < kMaxProbe; ++i) {
-        Header h = load_hdr(t.hdr + b);
+        const Header h = load_hdr_cg(t.hdr + b);
         if (h.epoch != ep) return -1;
         if (h.group == G) return (long long)b;
         b = (b + 1) & t.mask;
@@ -88,11 +90,12 @@ __device__ __forceinline__ long long lookup_group(const TableDev& t, unsigned ep
     return -1;
 }
 
-// Claim (or find) the bucket of group G in a table being written with epoch ep. Linear
-// probing with a 128-bit CAS per attempt; bounded. -1 and ST_TABLE_FULL when no bucket
-// within kMaxProbe of the home bucket is free.
+// Claim (or find) the bucket of group G: linear probing with a 128-bit CAS per attempt,
+// bounded. *created tells whether this call turned the bucket live. -1 and ST_TABLE_FULL
+// when no bucket within kMaxProbe of the home bucket is free.
 __device__ __forceinline__ long long claim_group(const TableDev& t, unsigned ep, unsigned long long G,
-                                                 unsigned int* status) {
+                                                 unsigned int* status, bool* created) {
+    *created = false;
     unsigned long long b = mix64(G) & t.mask;
     Header cur = load_hdr_cg(t.hdr + b);
     uint32_t probes = 0, attempts = 0;
@@ -107,8 +110,11 @@ __device__ __forceinline__ long long claim_group(const TableDev& t, unsigned ep,
         }
         Header want;
         want.group = G; want.epoch = ep; want.aux = 0;
-        Header old = cas_hdr(t.hdr + b, cur, want);
-        if (old.group == cur.group && old.epoch == cur.epoch && old.aux == cur.aux) return (long long)b;
+        const Header old = cas_hdr(t.hdr + b, cur, want);
+        if (old.group == cur.group && old.epoch == cur.epoch && old.aux == cur.aux) {
+            *created = true;
+            return (long long)b;
+        }
         cur = old;   // re-examine this bucket with its actual content
     }
     atomicCAS(status, 0u, (unsigned)ST_TABLE_FULL);
@@ -135,11 +141,20 @@ template <> struct Arith<float> {
 template <class T> struct Cx { T r, i; };
 
 // Sign flips and magnitude tests as integer operations: on this GPU every FP64 instruction,
-// compares and negations included, issues on the slow FP64 pipe. Both forms are exact.
+// compares and negations included, issues on the slow FP64 pipe. Both forms are exact. The
+// flip is an opaque integer xor on the high word, so the compiler cannot turn it back into
+// a floating-point negation (which it may lower to an FP64 add).
 __device__ __forceinline__ double neg(double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+    int hi = __double2hiint(x);
+    const int lo = __double2loint(x);
+    asm("xor.b32 %0, %0, 0x80000000;" : "+r"(hi));
+    return __hiloint2double(hi, lo);
 }
-__device__ __forceinline__ float neg(float x) { return __int_as_float(__float_as_int(x) ^ (int)0x80000000u); }
+__device__ __forceinline__ float neg(float x) {
+    int v = __float_as_int(x);
+    asm("xor.b32 %0, %0, 0x80000000;" : "+r"(v));
+    return __int_as_float(v);
+}
 
 // Coefficients are read through a pointer to the (L1-cached, warp-broadcast) descriptor.
 template <class T> struct Coef;
@@ -154,12 +169,9 @@ template <> struct Coef<float> {
     __device__ static __forceinline__ float m(const GateDesc* g, int i) { return __ldg(&g->mf[i]); }
 };
 
-template <class T>
-__device__ __forceinline__ Cx<T> cx_sel(bool p, Cx<T> a, Cx<T> b) { return p ? a : b; }
-
 // Branching update seen from one member of a pair: a = own amplitude, b = partner amplitude,
-// bit = own target bit. Each form below rounds exactly like the reference's pair formula for
-// that member (a + (-b) == a - b and (-s)*x == -(s*x) hold exactly in IEEE arithmetic):
+// bit = own logical target bit. Each form rounds exactly like the reference's pair formula
+// for that member (a + (-b) == a - b and (-s)*x == -(s*x) hold exactly in IEEE arithmetic):
 //   H : bit 0 -> f*(v0 + v1),             bit 1 -> f*(v0 - v1)
 //   Rx: c*own + s*(i-rotated partner)      (symmetric in the two members)
 //   Ry: bit 0 -> c*v0 - s*v1,             bit 1 -> c*v1 + s*v0
@@ -171,8 +183,8 @@ __device__ __forceinline__ Cx<T> branch_update(uint32_t kind, const GateDesc* g,
     switch (kind) {
     case KH: {
         const T f = Coef<T>::c(g);
-        Cx<T> x = bit ? b : a;
-        Cx<T> y = bit ? Cx<T>{neg(a.r), neg(a.i)} : b;
+        const Cx<T> x = bit ? b : a;
+        const Cx<T> y = bit ? Cx<T>{neg(a.r), neg(a.i)} : b;
         o.r = A::mul(f, A::add(x.r, y.r));
         o.i = A::mul(f, A::add(x.i, y.i));
         break;
@@ -211,6 +223,7 @@ __device__ __forceinline__ Cx<T> diag_update(uint32_t kind, const GateDesc* g, b
     case KZ: return bit ? Cx<T>{neg(a.r), neg(a.i)} : a;
     case KS: return bit ? Cx<T>{neg(a.i), a.r} : a;
     case KSDG: return bit ? Cx<T>{a.i, neg(a.r)} : a;
+    case KYPH: return bit ? Cx<T>{neg(a.i), a.r} : Cx<T>{a.i, neg(a.r)};
     case KRZ: {
         const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
         const T s = bit ? s0 : neg(s0);   // bit 0: conj(a)*v0, bit 1: a*v1
@@ -233,6 +246,11 @@ __device__ __forceinline__ Cx<T> swap_update(uint32_t kind, bool bit, Cx<T> b) {
 
 __device__ __forceinline__ bool is_branch(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
 __device__ __forceinline__ bool is_swap(uint32_t k) { return k == KX || k == KY; }
+// Diagonal kinds whose bit-0 member is unchanged: the whole warp can skip them when no lane
+// holds a satisfied bit-1 member.
+__device__ __forceinline__ bool is_one_sided(uint32_t k) {
+    return k == KZ || k == KS || k == KSDG || k == KPHASE || k == KT || k == KTDG;
+}
 
 // Prune rule of the reference (emulator/include/data_t.h:50-60): |re| < thr && |im| < thr,
 // decided in FP64. For doubles |x| < thr is compared on the bit patterns (non-negative

@@ -1,5 +1,5 @@
-// Host engine: table sizing and growth, pass planning, descriptor upload, deferred status
-// checks with replay. See sqc_engine.h.
+// Host engine: table sizing and growth, gate resolution and pass planning, descriptor upload,
+// deferred status checks with replay. See sqc_engine.h.
 #include "sqc_engine.h"
 
 #include <algorithm>
@@ -16,6 +16,7 @@ namespace {
 constexpr unsigned long long kMinBuckets = 64;
 constexpr size_t kFlushAt = 1024;          // queued gates that trigger a launch
 constexpr size_t kDescInitial = 1 << 14;   // descriptors held between verified syncs
+constexpr double kMaxLoad = 0.9;           // live buckets a pair pass may leave behind
 
 unsigned long long pow2_at_least(unsigned long long x) {
     unsigned long long p = 1;
@@ -24,15 +25,20 @@ unsigned long long pow2_at_least(unsigned long long x) {
 }
 
 bool is_diag_kind(uint32_t k) {
-    return k == SQC_Z || k == SQC_PHASE || k == SQC_RZ || k == SQC_S || k == SQC_SDG || k == SQC_T || k == SQC_TDG;
+    return k == KZ || k == KPHASE || k == KRZ || k == KS || k == KSDG || k == KT || k == KTDG || k == KYPH;
 }
-bool is_swap_kind(uint32_t k) { return k == SQC_X || k == SQC_Y; }
+bool is_one_sided_kind(uint32_t k) {
+    return k == KZ || k == KPHASE || k == KS || k == KSDG || k == KT || k == KTDG;
+}
+bool is_branch_kind(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
+bool is_swap_kind(uint32_t k) { return k == KX || k == KY; }
+bool streamable(const GateDesc& d) { return d.target < (uint32_t)kSlotBits || is_diag_kind(d.kind); }
 
 }  // namespace
 
 Engine::~Engine() {
     if (stream_) cudaStreamSynchronize(stream_);
-    free_tables(tab_);
+    free_table(&tab_);
     if (ctl_) cudaFree(ctl_);
     if (ctl_host_) cudaFreeHost(ctl_host_);
     if (d_desc_) cudaFree(d_desc_);
@@ -55,8 +61,10 @@ int Engine::cuda(cudaError_t e, const char* what) {
 }
 
 size_t Engine::bucket_bytes() const {
-    return sizeof(Header) + kSlots * sizeof(unsigned long long) + kSlots * (dbl_ ? 16 : 8);
+    return sizeof(Header) + kSlots * sizeof(unsigned long long) + kSlots * (dbl_ ? 16 : 8) + sizeof(unsigned);
 }
+
+unsigned long long Engine::max_groups() const { return (unsigned long long)(kMaxLoad * (double)tab_.nb); }
 
 int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt) {
     sqc_options o;
@@ -65,7 +73,7 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     if (nq < 1 || nq > 64) return fail(SQC_ERR_ARG, "nq must be in 1..64");
     if (o.precision != SQC_FP64 && o.precision != SQC_FP32) return fail(SQC_ERR_ARG, "precision must be 64 or 32");
     if (!(o.prune_threshold > 0.0)) return fail(SQC_ERR_ARG, "prune_threshold must be > 0");
-    if (!(o.load_factor > 0.0 && o.load_factor <= 0.9)) return fail(SQC_ERR_ARG, "load_factor must be in (0, 0.9]");
+    if (!(o.load_factor > 0.0 && o.load_factor <= kMaxLoad)) return fail(SQC_ERR_ARG, "load_factor must be in (0, 0.9]");
     double reserve = 0.05;
     if (params) {
         if (params->N_devices != 1) return fail(SQC_ERR_NO_DEVICE, "one GPU per state: N_devices must be 1");
@@ -95,7 +103,6 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
         own_stream_ = true;
     }
 
-    prune_.d = 0;
     std::memcpy(&prune_.d, &thr_, sizeof(double));
     float tf = (float)thr_;
     if ((double)tf >= thr_) tf = std::nextafter(tf, 0.0f);
@@ -107,54 +114,51 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     std::memset(ctl_host_, 0, sizeof(Ctl));
     if ((rc = ensure_desc(kDescInitial))) return rc;
 
-    unsigned long long nb = pow2_at_least(std::max<unsigned long long>(o.initial_buckets ? o.initial_buckets : 1024, kMinBuckets));
-    if ((rc = alloc_tables(nb, tab_))) return rc;
+    const unsigned long long nb =
+        pow2_at_least(std::max<unsigned long long>(o.initial_buckets ? o.initial_buckets : 1024, kMinBuckets));
+    if ((rc = alloc_table(nb, &tab_))) return rc;
     return set_zero();
 }
 
-int Engine::alloc_tables(unsigned long long nb, HostTable out[2]) {
-    if ((double)nb * bucket_bytes() * 2.0 > (double)budget_)
+int Engine::alloc_table(unsigned long long nb, HostTable* out) {
+    if ((double)nb * bucket_bytes() > (double)budget_)
         return fail(SQC_ERR_BUDGET, "table memory would exceed the HBM budget");
-    for (int i = 0; i < 2; ++i) {
-        HostTable t;
-        t.nb = nb;
-        int rc;
-        if ((rc = cuda(cudaMalloc(&t.hdr, nb * sizeof(Header)), "cudaMalloc(hdr)")) ||
-            (rc = cuda(cudaMalloc(&t.keys, nb * kSlots * sizeof(unsigned long long)), "cudaMalloc(keys)")) ||
-            (rc = cuda(cudaMalloc(&t.amps, nb * kSlots * (dbl_ ? 16 : 8)), "cudaMalloc(amps)")) ||
-            (rc = cuda(cudaMemsetAsync(t.hdr, 0, nb * sizeof(Header), stream_), "cudaMemset(hdr)"))) {
-            if (t.hdr) cudaFree(t.hdr);
-            if (t.keys) cudaFree(t.keys);
-            if (t.amps) cudaFree(t.amps);
-            if (i == 1) free_tables(out);
-            return rc;
-        }
-        out[i] = t;
+    HostTable t;
+    t.nb = nb;
+    int rc;
+    if ((rc = cuda(cudaMalloc(&t.hdr, nb * sizeof(Header)), "cudaMalloc(hdr)")) ||
+        (rc = cuda(cudaMalloc(&t.keys, nb * kSlots * sizeof(unsigned long long)), "cudaMalloc(keys)")) ||
+        (rc = cuda(cudaMalloc(&t.amps, nb * kSlots * (dbl_ ? 16 : 8)), "cudaMalloc(amps)")) ||
+        (rc = cuda(cudaMalloc(&t.list, nb * sizeof(unsigned)), "cudaMalloc(list)")) ||
+        (rc = cuda(cudaMemsetAsync(t.hdr, 0, nb * sizeof(Header), stream_), "cudaMemset(hdr)"))) {
+        free_table(&t);
+        return rc;
     }
+    *out = t;
     return SQC_OK;
 }
 
-void Engine::free_tables(HostTable t[2]) {
-    for (int i = 0; i < 2; ++i) {
-        if (t[i].hdr) cudaFree(t[i].hdr);
-        if (t[i].keys) cudaFree(t[i].keys);
-        if (t[i].amps) cudaFree(t[i].amps);
-        t[i] = HostTable();
-    }
+void Engine::free_table(HostTable* t) {
+    if (t->hdr) cudaFree(t->hdr);
+    if (t->keys) cudaFree(t->keys);
+    if (t->amps) cudaFree(t->amps);
+    if (t->list) cudaFree(t->list);
+    *t = HostTable();
 }
 
-TableDev Engine::dev(const HostTable& t) const {
+TableDev Engine::dev() const {
     TableDev d;
-    d.hdr = t.hdr;
-    d.keys = t.keys;
-    d.amps = t.amps;
-    d.mask = t.nb - 1;
+    d.hdr = tab_.hdr;
+    d.keys = tab_.keys;
+    d.amps = tab_.amps;
+    d.list = tab_.list;
+    d.mask = tab_.nb - 1;
     return d;
 }
 
 int Engine::ensure_desc(size_t n) {
     if (n <= desc_cap_) return SQC_OK;
-    size_t cap = std::max(n, desc_cap_ * 2);
+    const size_t cap = std::max(n, desc_cap_ * 2);
     if (d_desc_) cudaFree(d_desc_);
     if (h_desc_) cudaFreeHost(h_desc_);
     d_desc_ = nullptr;
@@ -169,7 +173,7 @@ int Engine::ensure_desc(size_t n) {
 
 int Engine::ensure_readout(size_t n) {
     if (n <= rcap_) return SQC_OK;
-    size_t cap = std::max<size_t>(n, 1024);
+    const size_t cap = std::max<size_t>(n, 1024);
     if (d_rk_) cudaFree(d_rk_);
     if (d_rr_) cudaFree(d_rr_);
     if (d_ri_) cudaFree(d_ri_);
@@ -183,24 +187,27 @@ int Engine::ensure_readout(size_t n) {
     return SQC_OK;
 }
 
-GateDesc Engine::resolve(const sqc_gate& g) const {
+// Descriptor of one device gate in the stored-key frame, coefficients resolved on the host.
+GateDesc Engine::make_desc(uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g) const {
     GateDesc d;
     std::memset(&d, 0, sizeof d);
-    d.kind = g.kind;
-    d.target = g.target;
-    d.ctrl = g.controls;
-    switch (g.kind) {
-    case SQC_PHASE: d.c = std::cos(g.theta); d.s = std::sin(g.theta); break;
-    case SQC_RZ: case SQC_RX: case SQC_RY: {
+    d.kind = kind;
+    d.target = target;
+    d.ctrl = ctrl;
+    d.cval = ctrl & ~plan_.frame;
+    d.flip = (uint32_t)((plan_.frame >> target) & 1ULL);
+    switch (kind) {
+    case KPHASE: d.c = std::cos(g.theta); d.s = std::sin(g.theta); break;
+    case KRZ: case KRX: case KRY: {
         const double h = g.theta / 2.;   // the reference passes par/2 (table_manager.cuh:333-336)
         d.c = std::cos(h);
         d.s = std::sin(h);
         break;
     }
-    case SQC_T: d.c = 0.70710678118654752440; d.s = 0.70710678118654752440; break;
-    case SQC_TDG: d.c = 0.70710678118654752440; d.s = -0.70710678118654752440; break;
-    case SQC_H: d.c = 1. / std::sqrt(2.); break;   // as in h_core (device_data.cuh:205)
-    case SQC_U: {
+    case KT: d.c = 0.70710678118654752440; d.s = 0.70710678118654752440; break;
+    case KTDG: d.c = 0.70710678118654752440; d.s = -0.70710678118654752440; break;
+    case KH: d.c = 1. / std::sqrt(2.); break;   // as in h_core (device_data.cuh:205)
+    case KU: {
         const double c = std::cos(g.theta / 2.), s = std::sin(g.theta / 2.);
         const double cl = std::cos(g.lambda), sl = std::sin(g.lambda);
         const double cp = std::cos(g.phi), sp = std::sin(g.phi);
@@ -219,11 +226,26 @@ GateDesc Engine::resolve(const sqc_gate& g) const {
     return d;
 }
 
-bool Engine::streamable(const sqc_gate& g) const {
-    if (g.target < (uint32_t)kSlotBits) return true;
-    if (is_diag_kind(g.kind)) return true;
-    if (is_swap_kind(g.kind)) return (g.controls & 0xFULL) == 0;
-    return false;
+// Resolve one gate against what the host knows of the keys. Returns true and a descriptor
+// when the gate needs the device; otherwise the gate was applied here (identity, or an
+// uncontrolled X as a frame flip) and is credited to the next device gate.
+bool Engine::plan_gate(const sqc_gate& g, GateDesc* out) {
+    Planner& p = plan_;
+    const unsigned long long bq = 1ULL << g.target;
+    const unsigned long long kc = g.controls & p.kmask;
+    if ((p.kval & kc) != kc) { ++p.credit; return false; }   // a control is known to be 0
+    const unsigned long long ctrl = g.controls & ~p.kmask;   // controls still to test per key
+    if (is_swap_kind(g.kind) && ctrl == 0) {
+        p.frame ^= bq;
+        if (p.kmask & bq) p.kval ^= bq;
+        if (g.kind == KX) { ++p.credit; return false; }
+        *out = make_desc(KYPH, g.target, 0, g);   // Y = relabel + diag(-i, +i)
+        return true;
+    }
+    if (is_one_sided_kind(g.kind) && (p.kmask & bq) && !(p.kval & bq)) { ++p.credit; return false; }
+    *out = make_desc(g.kind, g.target, ctrl, g);
+    if (is_branch_kind(g.kind) || is_swap_kind(g.kind)) p.kmask &= ~bq;
+    return true;
 }
 
 int Engine::set_zero() {
@@ -232,31 +254,38 @@ int Engine::set_zero() {
     passes_.clear();
     seq_verified_ = 0;
     desc_used_ = 0;
-    parity_ = 0;
-    int rc = cuda(launch_set_zero(dev(tab_[0]), ctl_, 0, dbl_, stream_), "set_zero");
+    plan_ = Planner();
+    snap_plan_ = plan_;
+    snap_log_ = 0;
+    host_upd_ = 0;
+    list_hint_ = 1;
+    int rc = cuda(launch_set_zero(dev(), ctl_, dbl_, stream_), "set_zero");
     ++launches_;
     return rc;
 }
 
 int Engine::set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n) {
     if (n && (!keys || !re || !im)) return fail(SQC_ERR_ARG, "null array");
-    for (uint64_t i = 0; i < n; ++i)
+    unsigned long long all_and = ~0ULL, all_or = 0;
+    for (uint64_t i = 0; i < n; ++i) {
         if (nq_ < 64 && (keys[i] >> nq_)) return fail(SQC_ERR_ARG, "key does not fit in nq bits");
+        all_and &= keys[i];
+        all_or |= keys[i];
+    }
     int rc;
-    // Wait for anything in flight, then size the tables for n keys in n groups at worst.
     if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
     pending_.clear();
     log_.clear();
     passes_.clear();
     seq_verified_ = 0;
     desc_used_ = 0;
-    unsigned long long need = pow2_at_least(std::max<unsigned long long>(kMinBuckets, (unsigned long long)std::ceil(n / lf_)));
-    if (need > tab_[0].nb) {
-        HostTable nt[2];
-        if ((rc = alloc_tables(need, nt))) return rc;
-        free_tables(tab_);
-        tab_[0] = nt[0];
-        tab_[1] = nt[1];
+    const unsigned long long need =
+        pow2_at_least(std::max<unsigned long long>(kMinBuckets, (unsigned long long)std::ceil((double)n / lf_)));
+    if (need > tab_.nb) {
+        HostTable nt;
+        if ((rc = alloc_table(need, &nt))) return rc;
+        free_table(&tab_);
+        tab_ = nt;
     }
     if ((rc = ensure_readout(n))) return rc;
     if (n) {
@@ -265,23 +294,26 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
             (rc = cuda(cudaMemcpyAsync(d_ri_, im, n * 8, cudaMemcpyHostToDevice, stream_), "H2D im")))
             return rc;
     }
-    parity_ = 0;
-    if ((rc = cuda(cudaMemsetAsync(&ctl_->nnz[0], 0, sizeof(unsigned long long), stream_), "memset")) ||
-        (rc = cuda(cudaMemsetAsync(&ctl_->groups[0], 0, sizeof(unsigned long long), stream_), "memset")))
-        return rc;
-    rc = cuda(launch_set_state(d_rk_, d_rr_, d_ri_, n, dev(tab_[0]), ctl_, 0, dbl_, sms_, stream_), "set_state");
-    launches_ += n ? 5 : 3;
+    plan_ = Planner();
+    if (n) {
+        plan_.kmask = ~(all_and ^ all_or);
+        plan_.kval = all_and & plan_.kmask;
+    }
+    snap_plan_ = plan_;
+    snap_log_ = 0;
+    host_upd_ = 0;
+    list_hint_ = std::max<unsigned long long>(n, 1);
+    rc = cuda(launch_set_state(d_rk_, d_rr_, d_ri_, n, dev(), ctl_, dbl_, sms_, stream_), "set_state");
+    launches_ += n ? 5 : 2;
     if (rc) return rc;
     if ((rc = read_ctl())) return rc;
-    if (ctl_host_->status == ST_DUPLICATE) {
-        set_zero();
-        return fail(SQC_ERR_ARG, "duplicate key in set_state");
-    }
     if (ctl_host_->status != ST_OK) {
+        const bool dup = ctl_host_->status == ST_DUPLICATE;
         set_zero();
-        return fail(SQC_ERR_TABLE_FULL, "set_state: table full");
+        return dup ? fail(SQC_ERR_ARG, "duplicate key in set_state") : fail(SQC_ERR_TABLE_FULL, "set_state: table full");
     }
     seq_verified_ = ctl_host_->seq;
+    list_hint_ = std::max<unsigned long long>(ctl_host_->list_n, 1);
     return SQC_OK;
 }
 
@@ -299,19 +331,8 @@ int Engine::apply(const sqc_gate* gates, uint64_t n) {
     return SQC_OK;
 }
 
-PassArgs Engine::pass_args() const {
-    PassArgs a;
-    std::memset(&a, 0, sizeof a);
-    a.tab[0] = dev(tab_[0]);
-    a.tab[1] = dev(tab_[1]);
-    a.ctl = ctl_;
-    a.amp_bytes = dbl_ ? 16u : 8u;
-    a.prune = prune_;
-    return a;
-}
-
-// Split the queued gates into passes and launch them. A pass is either a run of streamable
-// gates, or one cross-group gate followed by a run of streamable gates.
+// Resolve the queued gates, split the device gates into passes and launch them. A pass is
+// either a run of streamable gates, or one cross-group gate followed by such a run.
 int Engine::flush() {
     if (pending_.empty()) return SQC_OK;
     const size_t n = pending_.size();
@@ -319,41 +340,62 @@ int Engine::flush() {
     if (desc_used_ + n > desc_cap_) {
         std::vector<sqc_gate> keep;
         keep.swap(pending_);
-        if ((rc = sync())) return rc;          // verifies everything launched, resets desc_used_
+        if ((rc = sync())) return rc;   // verifies everything launched, resets desc_used_
         pending_.swap(keep);
         if ((rc = ensure_desc(n))) return rc;
     }
+    const size_t log_base = log_.size();
+    log_.insert(log_.end(), pending_.begin(), pending_.end());
     GateDesc* hd = h_desc_ + desc_used_;
-    for (size_t i = 0; i < n; ++i) hd[i] = resolve(pending_[i]);
-    if ((rc = cuda(cudaMemcpyAsync(d_desc_ + desc_used_, hd, n * sizeof(GateDesc), cudaMemcpyHostToDevice, stream_),
+    std::vector<size_t> src;
+    std::vector<Planner> after;
+    src.reserve(n);
+    after.reserve(n);
+    size_t nd = 0;
+    for (size_t i = 0; i < n; ++i) {
+        GateDesc d;
+        if (!plan_gate(pending_[i], &d)) continue;
+        d.pad = plan_.credit;
+        plan_.credit = 0;
+        hd[nd++] = d;
+        src.push_back(log_base + i);
+        after.push_back(plan_);
+    }
+    gates_applied_ += n;
+    pending_.clear();
+    if (nd == 0) return SQC_OK;
+    if ((rc = cuda(cudaMemcpyAsync(d_desc_ + desc_used_, hd, nd * sizeof(GateDesc), cudaMemcpyHostToDevice, stream_),
                    "H2D gate descriptors")))
         return rc;
-    const uint32_t log_base = (uint32_t)log_.size();
-    log_.insert(log_.end(), pending_.begin(), pending_.end());
-    PassArgs a = pass_args();
+    PassArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.t = dev();
+    a.ctl = ctl_;
     a.gates = d_desc_ + desc_used_;
+    a.amp_bytes = dbl_ ? 16u : 8u;
+    a.max_groups = max_groups();
+    a.prune = prune_;
     size_t i = 0;
-    while (i < n) {
+    while (i < nd) {
         const size_t start = i;
-        const bool pair = !streamable(pending_[i]);
+        const bool pair = !streamable(hd[i]);
         if (pair) ++i;
-        while (i < n && i - start < max_run_ && streamable(pending_[i])) ++i;
+        while (i < nd && i - start < max_run_ && streamable(hd[i])) ++i;
+        bool fixed = true;
+        for (size_t k = start; k < i; ++k) fixed = fixed && is_diag_kind(hd[k].kind);
         a.g0 = (uint32_t)start;
         a.g1 = (uint32_t)i;
-        a.parity = (uint32_t)parity_;
         a.pair = pair ? 1u : 0u;
-        bool fixed = true;
-        for (size_t j = start; j < i; ++j) fixed = fixed && is_diag_kind(pending_[j].kind);
         a.keys_fixed = fixed ? 1u : 0u;
-        if ((rc = cuda(launch_pass(a, dbl_, sms_, stream_), "gate pass"))) return rc;
-        passes_.push_back(PassRec{log_base + (uint32_t)start, (uint32_t)(i - start), parity_, pair});
-        parity_ ^= 1;
+        if (pair) list_hint_ = std::min<unsigned long long>(tab_.nb, 2 * list_hint_);
+        if ((rc = cuda(launch_pass(a, list_hint_, dbl_, sms_, stream_), "gate pass"))) return rc;
+        passes_.push_back(PassRec{snap_log_, snap_plan_});
+        snap_log_ = src[i - 1] + 1;
+        snap_plan_ = after[i - 1];
         ++launches_;
         ++passes_run_;
     }
-    gates_applied_ += n;
-    desc_used_ += n;
-    pending_.clear();
+    desc_used_ += nd;
     return SQC_OK;
 }
 
@@ -369,58 +411,85 @@ int Engine::sync() {
     for (int attempt = 0; attempt < 64; ++attempt) {
         if ((rc = flush())) return rc;
         if ((rc = read_ctl())) return rc;
-        if (ctl_host_->status == ST_OK) {
+        const unsigned st = ctl_host_->status;
+        if (st == ST_OK) {
+            host_upd_ += (unsigned long long)plan_.credit * ctl_host_->nnz;
+            plan_.credit = 0;
             seq_verified_ = ctl_host_->seq;
             log_.clear();
             passes_.clear();
             desc_used_ = 0;
+            snap_log_ = 0;
+            snap_plan_ = plan_;
+            list_hint_ = std::max<unsigned long long>(ctl_host_->list_n, 1);
+            // many groups left without keys (pruned away): rebuild without them
+            if (ctl_host_->list_n > 4096 && ctl_host_->empty_groups * 2 > ctl_host_->list_n) {
+                if ((rc = rebuild(tab_.nb))) return rc;
+            }
             return SQC_OK;
         }
-        if (ctl_host_->status != ST_TABLE_FULL) return fail(SQC_ERR_STATE, "device status error");
+        if (st != ST_GROW) {
+            return fail(st == ST_TABLE_FULL ? SQC_ERR_TABLE_FULL : SQC_ERR_STATE,
+                        "device status " + std::to_string(st) + ": the state is no longer valid; reset it");
+        }
         const size_t k = (size_t)(ctl_host_->seq - seq_verified_);
-        if (k >= passes_.size()) return fail(SQC_ERR_STATE, "table full outside a gate pass");
+        if (k >= passes_.size()) return fail(SQC_ERR_STATE, "growth request outside a gate pass");
         if ((rc = repair(k))) return rc;
     }
     return fail(SQC_ERR_TABLE_FULL, "table growth did not converge");
 }
 
-// Pass k ran out of table space. Its input table is intact: move it into larger tables and
-// queue the gates of pass k and of every later pass again.
-int Engine::repair(size_t k) {
-    const PassRec pr = passes_[k];
-    const int pin = pr.parity_in;
-    const unsigned long long groups_in = ctl_host_->groups[pin];
-    unsigned long long nb = tab_[0].nb * 2;
-    nb = std::max(nb, pow2_at_least((unsigned long long)std::ceil(2.0 * (double)groups_in / lf_)));
-    HostTable nt[2];
+// Copy the live, non-empty buckets into a new table of nb_new buckets. The control block
+// must be in sync with the device (read_ctl) and no pass may be in flight.
+int Engine::rebuild(unsigned long long nb_new) {
+    HostTable nt;
     int rc;
-    if ((rc = alloc_tables(nb, nt))) return rc;
+    if ((rc = alloc_table(nb_new, &nt))) return rc;
+    const unsigned long long n_old = ctl_host_->list_n;
     Ctl c = *ctl_host_;
-    const unsigned ep_old = c.epoch[pin];
-    std::memset(&c, 0, sizeof c);
-    c.epoch[0] = 1;
-    c.epoch[1] = 0;
-    c.nnz[0] = ctl_host_->nnz[pin];
-    c.groups[0] = ctl_host_->groups[pin];
-    c.amp_updates = ctl_host_->amp_updates;
-    c.alg_bytes = ctl_host_->alg_bytes;
+    c.epoch = 1;
+    c.status = 0;
+    c.done = 0;
+    c.seq = 0;
+    c.list_n = 0;
+    c.list_tail = 0;
+    c.empty_groups = 0;
+    c.acc_nnz = c.acc_empty = c.acc_upd = 0;
     std::memcpy(ctl_host_, &c, sizeof c);
     if ((rc = cuda(cudaMemcpyAsync(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice, stream_), "H2D ctl")))
         return rc;
-    if ((rc = cuda(launch_rehash(dev(tab_[pin]), ep_old, dev(nt[0]), 1u, dbl_ ? 16 : 8, ctl_, sms_, stream_),
-                   "rehash")))
-        return rc;
+    TableDev nd;
+    nd.hdr = nt.hdr; nd.keys = nt.keys; nd.amps = nt.amps; nd.list = nt.list; nd.mask = nt.nb - 1;
+    if ((rc = cuda(launch_rehash(dev(), n_old, nd, 1u, dbl_ ? 16 : 8, ctl_, sms_, stream_), "rehash"))) return rc;
     ++launches_;
     if ((rc = read_ctl())) return rc;
     if (ctl_host_->status != ST_OK) {
-        free_tables(nt);
-        return fail(SQC_ERR_TABLE_FULL, "rehash into the grown table failed");
+        free_table(&nt);
+        return fail(SQC_ERR_TABLE_FULL, "rebuild into the new table failed");
     }
-    free_tables(tab_);
-    tab_[0] = nt[0];
-    tab_[1] = nt[1];
-    parity_ = 0;
-    std::vector<sqc_gate> again(log_.begin() + pr.first_gate, log_.end());
+    ctl_host_->list_n = ctl_host_->list_tail;
+    if ((rc = cuda(cudaMemcpyAsync(&ctl_->list_n, &ctl_host_->list_n, sizeof(unsigned long long),
+                                   cudaMemcpyHostToDevice, stream_), "H2D list_n")) ||
+        (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
+        return rc;
+    free_table(&tab_);
+    tab_ = nt;
+    seq_verified_ = 0;
+    list_hint_ = std::max<unsigned long long>(ctl_host_->list_n, 1);
+    ++rebuilds_;
+    return SQC_OK;
+}
+
+// Pass k refused to start because the table might overflow. Nothing of it ran; the state
+// is the output of pass k-1. Grow the table and queue pass k's gates (and all later ones)
+// again, from the planner state saved with pass k.
+int Engine::repair(size_t k) {
+    const PassRec pr = passes_[k];
+    const unsigned long long groups = ctl_host_->list_n;
+    const unsigned long long nb = std::max(tab_.nb * 2, pow2_at_least((unsigned long long)std::ceil(4.0 * (double)groups / kMaxLoad)));
+    int rc;
+    if ((rc = rebuild(nb))) return rc;
+    std::vector<sqc_gate> again(log_.begin() + (long)pr.log_begin, log_.end());
     replays_ += passes_.size() - k;
     passes_run_ -= passes_.size() - k;
     gates_applied_ -= again.size();
@@ -428,6 +497,9 @@ int Engine::repair(size_t k) {
     passes_.clear();
     seq_verified_ = 0;
     desc_used_ = 0;
+    plan_ = pr.snap;
+    snap_plan_ = plan_;
+    snap_log_ = 0;
     again.insert(again.end(), pending_.begin(), pending_.end());
     pending_.swap(again);
     return SQC_OK;
@@ -436,17 +508,17 @@ int Engine::repair(size_t k) {
 int Engine::nnz(uint64_t* out) {
     int rc = sync();
     if (rc) return rc;
-    *out = ctl_host_->nnz[parity_];
+    *out = ctl_host_->nnz;
     return SQC_OK;
 }
 
 int Engine::get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
     int rc = sync();
     if (rc) return rc;
-    const unsigned long long have = ctl_host_->nnz[parity_];
+    const unsigned long long have = ctl_host_->nnz;
     if ((rc = ensure_readout(have))) return rc;
     if ((rc = cuda(cudaMemsetAsync(&ctl_->out_count, 0, sizeof(unsigned long long), stream_), "memset"))) return rc;
-    if ((rc = cuda(launch_readout(dev(tab_[parity_]), ctl_, parity_, dbl_, d_rk_, d_rr_, d_ri_, rcap_,
+    if ((rc = cuda(launch_readout(dev(), ctl_, list_hint_, plan_.frame, dbl_, d_rk_, d_rr_, d_ri_, rcap_,
                                   (flags & SQC_READ_DROP_NEGLIGIBLE) != 0, prune_, sms_, stream_),
                    "readout")))
         return rc;
@@ -481,7 +553,7 @@ int Engine::norm2(double* out) {
     int rc = sync();
     if (rc) return rc;
     if ((rc = cuda(cudaMemsetAsync(&ctl_->acc[0], 0, sizeof(double), stream_), "memset"))) return rc;
-    if ((rc = cuda(launch_norm(dev(tab_[parity_]), ctl_, parity_, dbl_, sms_, stream_), "norm"))) return rc;
+    if ((rc = cuda(launch_norm(dev(), ctl_, list_hint_, dbl_, sms_, stream_), "norm"))) return rc;
     ++launches_;
     if ((rc = read_ctl())) return rc;
     *out = ctl_host_->acc[0];
@@ -490,14 +562,15 @@ int Engine::norm2(double* out) {
 
 int Engine::compare(Engine& b, double* fidelity, double* max_abs_err) {
     if (b.nq_ != nq_) return fail(SQC_ERR_ARG, "states differ in qubit count");
+    if (b.device_ != device_) return fail(SQC_ERR_ARG, "states live on different devices");
     int rc;
     if ((rc = b.sync())) return fail(rc, "compare: " + b.err);
     if ((rc = sync())) return rc;
     if ((rc = cuda(cudaMemsetAsync(ctl_->acc, 0, sizeof(ctl_->acc), stream_), "memset")) ||
         (rc = cuda(cudaMemsetAsync(&ctl_->acc_max, 0, sizeof(unsigned long long), stream_), "memset")))
         return rc;
-    if ((rc = cuda(launch_compare(dev(tab_[parity_]), ctl_host_->epoch[parity_], dbl_, b.dev(b.tab_[b.parity_]),
-                                  b.ctl_host_->epoch[b.parity_], b.dbl_, ctl_, sms_, stream_),
+    if ((rc = cuda(launch_compare(dev(), ctl_, list_hint_, dbl_, b.dev(), b.ctl_, b.list_hint_, b.dbl_,
+                                  plan_.frame ^ b.plan_.frame, ctl_, sms_, stream_),
                    "compare")))
         return rc;
     launches_ += 2;
@@ -516,10 +589,10 @@ int Engine::stats(sqc_stats* out) {
     out->gates_applied = gates_applied_;
     out->passes = passes_run_;
     out->kernel_launches = launches_;
-    out->buckets = tab_[0].nb;
-    out->table_bytes = (uint64_t)(tab_[0].nb * bucket_bytes() * 2);
+    out->buckets = tab_.nb;
+    out->table_bytes = (uint64_t)(tab_.nb * bucket_bytes());
     out->replays = replays_;
-    out->amp_updates = ctl_host_ ? ctl_host_->amp_updates : 0;
+    out->amp_updates = (ctl_host_ ? ctl_host_->amp_updates : 0) + host_upd_;
     out->alg_bytes = ctl_host_ ? ctl_host_->alg_bytes : 0;
     return SQC_OK;
 }

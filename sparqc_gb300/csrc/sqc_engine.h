@@ -1,5 +1,5 @@
-// Host engine of one sparse state on one GPU: owns the two tables, the device control block,
-// the gate-descriptor buffer and the pass planner. Replaces the reference's TableManager__
+// Host engine of one sparse state on one GPU: owns the table, the device control block, the
+// gate-descriptor buffer and the pass planner. Replaces the reference's TableManager__
 // (emulator/device/table_manager.cuh:45-353) and MappingFC__ launchers
 // (emulator/device/mapping_GHT.cuh:54-73).
 #pragma once
@@ -17,14 +17,24 @@ struct HostTable {
     Header* hdr = nullptr;
     unsigned long long* keys = nullptr;
     void* amps = nullptr;
+    unsigned int* list = nullptr;
     unsigned long long nb = 0;
 };
 
+// What the host knows about the keys without looking at them: stored key = actual key ^
+// frame; bits in kmask are identical across all keys and equal kval. Gates whose effect
+// follows from this are resolved here: an uncontrolled X flips a frame bit, a gate with a
+// known-zero control or a one-sided diagonal gate on a known-zero bit is the identity.
+struct Planner {
+    unsigned long long frame = 0;
+    unsigned long long kmask = ~0ULL;
+    unsigned long long kval = 0;
+    uint32_t credit = 0;   // resolved gates not yet credited to a device gate
+};
+
 struct PassRec {
-    uint32_t first_gate;   // index into log_
-    uint32_t ngates;
-    int parity_in;
-    bool pair;
+    size_t log_begin;   // replay of this pass starts at this log index...
+    Planner snap;       // ...with this planner state
 };
 
 class Engine {
@@ -38,8 +48,8 @@ public:
     int set_zero();
     int set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n);
     int apply(const sqc_gate* gates, uint64_t n);
-    int sync();
     int flush();
+    int sync();
     int nnz(uint64_t* out);
     int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
     int norm2(double* out);
@@ -54,16 +64,17 @@ private:
     int fail(int code, const std::string& msg);
     int cuda(cudaError_t e, const char* what);
     size_t bucket_bytes() const;
-    int alloc_tables(unsigned long long nb, HostTable out[2]);
-    void free_tables(HostTable t[2]);
-    TableDev dev(const HostTable& t) const;
-    PassArgs pass_args() const;
+    int alloc_table(unsigned long long nb, HostTable* out);
+    void free_table(HostTable* t);
+    TableDev dev() const;
+    int rebuild(unsigned long long nb_new);
     int repair(size_t failed_pass);
     int ensure_desc(size_t n);
     int ensure_readout(size_t n);
-    GateDesc resolve(const sqc_gate& g) const;
-    bool streamable(const sqc_gate& g) const;
+    bool plan_gate(const sqc_gate& g, GateDesc* out);
+    GateDesc make_desc(uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g) const;
     int read_ctl();
+    unsigned long long max_groups() const;
 
     int device_ = 0;
     int sms_ = 1;
@@ -76,12 +87,17 @@ private:
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;
 
-    HostTable tab_[2];
+    HostTable tab_;
     Ctl* ctl_ = nullptr;        // device
     Ctl* ctl_host_ = nullptr;   // pinned mirror
-    int parity_ = 0;            // table holding the state once every launched pass has run
     unsigned long long seq_verified_ = 0;
+    unsigned long long list_hint_ = 1;
     PruneBits prune_{};
+
+    Planner plan_;              // after every queued gate
+    Planner snap_plan_;         // right after the last launched device gate...
+    size_t snap_log_ = 0;       // ...whose source gate precedes this log index
+    unsigned long long host_upd_ = 0;   // amp updates credited on the host (resolved trailing gates)
 
     std::vector<sqc_gate> pending_;   // queued, not launched
     std::vector<sqc_gate> log_;       // launched since the last verified sync
@@ -96,7 +112,7 @@ private:
     double* d_ri_ = nullptr;
     size_t rcap_ = 0;
 
-    uint64_t gates_applied_ = 0, passes_run_ = 0, launches_ = 0, replays_ = 0;
+    uint64_t gates_applied_ = 0, passes_run_ = 0, launches_ = 0, replays_ = 0, rebuilds_ = 0;
 };
 
 }  // namespace sqc

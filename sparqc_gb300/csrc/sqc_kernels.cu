@@ -1,21 +1,26 @@
 // Gate-pass and bookkeeping kernels of the sparse statevector engine (sm_103a).
 //
-// One gate pass reads the input table and writes a fresh output table. Two pass shapes:
-//  * stream pass: a run of gates that never pair keys across 16-key groups -- diagonal
-//    gates on any qubit, any gate on qubits 0..3 (the partner is in the same bucket and is
-//    reached with a warp shuffle), and X/Y on a qubit >= 4 whose controls are all >= 4 (the
-//    whole group moves to G ^ (1 << (q-4)) or stays). Each half-warp streams one bucket.
+// A gate pass updates the table in place; it walks the list of live buckets.
+//  * stream pass: a run of gates that never pair keys across 16-key groups -- diagonal gates
+//    on any qubit and any gate on qubits 0..3 (the partner sits in the same bucket and is
+//    reached with a warp shuffle). Each half-warp streams two buckets (lane j holds slot j of
+//    both), so a warp keeps four buckets in flight.
 //  * pair pass: a gate whose partner key lives in another group (branching gate on a qubit
-//    >= 4, or X/Y on a qubit >= 4 with a control below 4), followed by a stream run. A warp
-//    takes the group pair (G0, G1 = G0 | m): lanes 0-15 hold G0's slots, 16-31 G1's; the
-//    partner of every lane is lane ^ 16. The group with target bit 0 owns the pair; the
-//    bit-1 group owns it only when its partner group is absent -- the reference's pair rule
-//    (emulator/device/device_table_FC.cuh:62-110) lifted from keys to 16-key groups, which
-//    yields the same pairs and the same per-key results.
-// Every pair with at least one present member is read once and written once. Pruning
-// follows the reference (emulator/device/device_data.cuh:108-156): branching gates drop
-// negligible outputs, swap and diagonal gates keep every key.
+//    >= 4, or X/Y on a qubit >= 4 with controls the host could not resolve), followed by a
+//    stream run. A half-warp takes the group pair (G0, G1 = G0 | m): lane j holds slot j of
+//    both groups, so the pair update is lane-local. The group with stored target bit 0 owns
+//    the pair; the other owns it only when its partner group is absent -- the reference's pair
+//    rule (emulator/device/device_table_FC.cuh:62-110) lifted from keys to 16-key groups,
+//    which gives the same pairs and the same per-key results. Ownership lookups of four list
+//    entries run in parallel; owned pairs are packed two per warp.
+// Every pair with at least one present member is read once and written back once, at the
+// same place. A group that appears for the first time is claimed with a 128-bit CAS and
+// appended to the list; such groups are not revisited in the same pass. Pruning follows the
+// reference (emulator/device/device_data.cuh:108-156): branching gates drop negligible
+// outputs, swap and diagonal gates keep every key.
 #include "sqc_kernels.h"
+
+#include <algorithm>
 
 namespace sqc {
 
@@ -27,108 +32,210 @@ template <> struct AmpT<float> { using V = float2; };
 
 template <class T>
 __device__ __forceinline__ Cx<T> load_amp(const void* amps, size_t s) {
-    typename AmpT<T>::V v = reinterpret_cast<const typename AmpT<T>::V*>(amps)[s];
+    const typename AmpT<T>::V v = reinterpret_cast<const typename AmpT<T>::V*>(amps)[s];
     return Cx<T>{v.x, v.y};
 }
 template <class T>
 __device__ __forceinline__ void store_amp(void* amps, size_t s, Cx<T> a) {
     typename AmpT<T>::V v;
-    v.x = a.r; v.y = a.i;
+    v.x = a.r;
+    v.y = a.i;
     reinterpret_cast<typename AmpT<T>::V*>(amps)[s] = v;
 }
 __device__ __forceinline__ Cx<double> load_amp_any(const void* amps, size_t s, bool dbl) {
-    if (dbl) { double2 v = reinterpret_cast<const double2*>(amps)[s]; return Cx<double>{v.x, v.y}; }
-    float2 v = reinterpret_cast<const float2*>(amps)[s];
+    if (dbl) { const double2 v = reinterpret_cast<const double2*>(amps)[s]; return Cx<double>{v.x, v.y}; }
+    const float2 v = reinterpret_cast<const float2*>(amps)[s];
     return Cx<double>{(double)v.x, (double)v.y};
 }
 
 template <class T> __device__ __forceinline__ Cx<T> czero() { return Cx<T>{T(0), T(0)}; }
 
-// One gate applied by one lane to its own slot. `off` is the lane distance to the partner
-// (1 << q for q < 4 inside a half-warp, 16 across the two halves of a pair pass), or 0 for a
-// gate that needs no partner (diagonal gate, or X/Y on a qubit >= 4 moving the whole group).
+__device__ __forceinline__ bool slot_present(unsigned long long key, int j) { return (int)(key & 15ULL) == j; }
+
+// One slot held by a lane: its group, amplitude and presence, where it lives (b = -1 for a
+// group absent at the start of the pass) and whether the pass changed it.
+template <class T> struct Val {
+    unsigned long long G;
+    long long b;
+    Cx<T> amp;
+    bool pres, pres0, dirty;
+};
+
 template <class T>
-__device__ __forceinline__ void gate_step(const GateDesc* g, uint32_t kind, uint32_t target,
-                                          unsigned long long ctrl, int off, unsigned long long& G, int j,
-                                          Cx<T>& amp, bool& pres, const PruneBits& pb) {
-    const unsigned long long key = (G << kSlotBits) | (unsigned long long)j;
-    const bool sat = (key & ctrl) == ctrl;
-    const bool bit = (key >> target) & 1ULL;
+__device__ __forceinline__ void load_val(const TableDev& t, Val<T>& v, unsigned long long G, long long b, int j) {
+    v.G = G;
+    v.b = b;
+    v.dirty = false;
+    v.pres = false;
+    v.amp = czero<T>();
+    if (b >= 0) {
+        const size_t s = (size_t)b * kSlots + j;
+        v.pres = slot_present(t.keys[s], j);
+        if (v.pres) v.amp = load_amp<T>(t.amps, s);
+    }
+    v.pres0 = v.pres;
+}
+
+struct GateHead {
+    uint32_t kind, target, flip, credit;
+    unsigned long long ctrl, cval;
+};
+
+__device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
+    GateHead h;
+    h.kind = __ldg(&g->kind);
+    h.target = __ldg(&g->target);
+    h.flip = __ldg(&g->flip);
+    h.credit = __ldg(&g->pad);
+    h.ctrl = __ldg(&g->ctrl);
+    h.cval = __ldg(&g->cval);
+    return h;
+}
+
+// One streamable gate on one held slot. `off` is the lane distance to the partner slot
+// (1 << q for q < 4, inside the half-warp) or 0 for a diagonal gate on a qubit >= 4.
+template <class T>
+__device__ __forceinline__ void gate_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
+                                          const PruneBits& pb) {
+    const unsigned long long key = (v.G << kSlotBits) | (unsigned long long)j;
+    const bool sat = (key & h.ctrl) == h.cval;
+    const bool bit = (((key >> h.target) & 1ULL) != 0) != (h.flip != 0);
     if (off) {
         Cx<T> pa;
-        pa.r = __shfl_xor_sync(kFull, amp.r, off);
-        pa.i = __shfl_xor_sync(kFull, amp.i, off);
-        const bool pp = __shfl_xor_sync(kFull, (int)pres, off) != 0;
-        if (is_swap(kind)) {
-            if (sat) { amp = swap_update<T>(kind, bit, pa); pres = pp; }
-        } else if (is_branch(kind)) {
-            const bool any = pres || pp;
+        pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
+        pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
+        const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
+        if (is_swap(h.kind)) {
+            if (sat) {
+                v.amp = swap_update<T>(h.kind, bit, pa);
+                v.pres = pp;
+                v.dirty = true;
+            }
+        } else if (is_branch(h.kind)) {
+            const bool any = v.pres || pp;
             if (__any_sync(kFull, sat && any)) {
-                const Cx<T> o = branch_update<T>(kind, g, bit, amp, pa);
+                const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
                 if (sat) {
                     const bool keep = any && !negligible(o, pb);
-                    pres = keep;
-                    amp = keep ? o : czero<T>();
+                    v.pres = keep;
+                    v.amp = keep ? o : czero<T>();
+                    v.dirty = true;
                 }
             }
-        } else if (__any_sync(kFull, sat && pres)) {
-            const Cx<T> o = diag_update<T>(kind, g, bit, amp);
-            if (sat) amp = o;
+        } else {
+            const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
+            if (__any_sync(kFull, need)) {
+                const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
+                if (need) { v.amp = o; v.dirty = true; }
+            }
         }
         return;
     }
-    if (is_swap(kind)) {           // target >= 4, controls >= 4: uniform over the group
-        if (sat) {
-            G ^= 1ULL << (target - kSlotBits);
-            amp = swap_update<T>(kind, !bit, amp);
-        }
-    } else if (__any_sync(kFull, sat && pres)) {
-        const Cx<T> o = diag_update<T>(kind, g, bit, amp);
-        if (sat) amp = o;
+    const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
+    if (__any_sync(kFull, need)) {
+        const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
+        if (need) { v.amp = o; v.dirty = true; }
     }
 }
 
-// Apply gates [g0, g1) to the lane's slot. In a pair pass the first gate pairs the halves.
+// The cross-group gate of a pair pass, lane-local: a = slot of G0 (stored bit 0), b = slot of G1.
+template <class T>
+__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b, int j,
+                                          const PruneBits& pb) {
+    const unsigned long long key = (a.G << kSlotBits) | (unsigned long long)j;
+    const bool sat = (key & h.ctrl) == h.cval;
+    const bool bit_a = h.flip != 0, bit_b = !bit_a;
+    if (is_swap(h.kind)) {
+        if (sat) {
+            const Cx<T> na = swap_update<T>(h.kind, bit_a, b.amp), nb = swap_update<T>(h.kind, bit_b, a.amp);
+            const bool pa = b.pres, pbr = a.pres;
+            a.amp = na; b.amp = nb;
+            a.pres = pa; b.pres = pbr;
+            a.dirty = b.dirty = true;
+        }
+        return;
+    }
+    const bool any = a.pres || b.pres;
+    if (__any_sync(kFull, sat && any)) {
+        const Cx<T> oa = branch_update<T>(h.kind, g, bit_a, a.amp, b.amp);
+        const Cx<T> ob = branch_update<T>(h.kind, g, bit_b, b.amp, a.amp);
+        if (sat) {
+            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+            a.pres = ka; a.amp = ka ? oa : czero<T>();
+            b.pres = kb; b.amp = kb ? ob : czero<T>();
+            a.dirty = b.dirty = true;
+        }
+    }
+}
+
+// Apply gates [g0, g1) to the two held slots; in a pair pass the first gate pairs them.
+// Lane 0 accumulates the amp-update count: every gate is credited with the present slots
+// it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
 template <class T>
 __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1,
-                                          bool pair_first, unsigned long long& G, int lane, Cx<T>& amp,
-                                          bool& pres, const PruneBits& pb, unsigned long long& upd) {
+                                          bool pair_first, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
+                                          unsigned long long& upd) {
     const int j = lane & 15;
-    const unsigned hmask = lane < 16 ? 0x0000FFFFu : 0xFFFF0000u;
     for (uint32_t gi = g0; gi < g1; ++gi) {
         const GateDesc* g = gates + gi;
-        const uint32_t kind = __ldg(&g->kind), target = __ldg(&g->target);
-        const unsigned long long ctrl = __ldg(&g->ctrl);
-        const unsigned bal = __ballot_sync(kFull, pres);
-        if (j == 0) upd += __popc(bal & hmask);
-        int off;
-        if (gi == g0 && pair_first) off = 16;
-        else if (target < (uint32_t)kSlotBits) off = 1 << target;
-        else off = 0;
-        gate_step<T>(g, kind, target, ctrl, off, G, j, amp, pres, pb);
+        const GateHead h = gate_head(g);
+        const unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        if (gi == g0 && pair_first) {
+            pair_step<T>(g, h, a, b, j, pb);
+            continue;
+        }
+        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : 0;
+        gate_step<T>(g, h, off, a, j, pb);
+        gate_step<T>(g, h, off, b, j, pb);
     }
 }
 
-// Write one half-warp's group into the output table: claim its bucket, write all 16 keys
-// (present key or EMPTY marker) and the present amplitudes. Nothing is written for a group
-// with no present key.
+// Write a held slot back in place. A group absent at the start of the pass gets a bucket
+// (claimed by lane 0 of the half) when it ends up with a present key; every slot of a new
+// bucket is written. Returns the new bucket index on lane 0 of the half, else -1.
 template <class T>
-__device__ __forceinline__ void write_group(const TableDev& tout, unsigned ep_out, unsigned long long G,
-                                            int lane, bool act, Cx<T> amp, bool pres, unsigned int* status,
-                                            unsigned long long& cnt_nnz, unsigned long long& cnt_groups) {
+__device__ __forceinline__ long long write_val(const TableDev& t, unsigned ep, Val<T>& v, int lane,
+                                               unsigned int* status, unsigned long long& cnt_nnz,
+                                               unsigned long long& cnt_empty) {
     const int j = lane & 15, half = lane >> 4;
-    const unsigned bal = __ballot_sync(kFull, pres && act);
+    const unsigned bal = __ballot_sync(kFull, v.pres);
     const unsigned hm = half ? (bal >> 16) : (bal & 0xFFFFu);
-    long long ob = -1;
-    if (j == 0 && hm) ob = claim_group(tout, ep_out, G, status);
-    ob = (long long)shfl64((unsigned long long)ob, half << 4);
-    if (hm && ob >= 0) {
-        const size_t s = (size_t)ob * kSlots + j;
-        tout.keys[s] = pres ? ((G << kSlotBits) | (unsigned long long)j) : empty_key(j);
-        if (pres) store_amp<T>(tout.amps, s, amp);
-        if (j == 0) cnt_groups += 1;
-        cnt_nnz += pres ? 1 : 0;
+    long long b = v.b;
+    bool created = false;
+    long long fresh = -1;
+    if (__any_sync(kFull, b < 0 && hm != 0)) {
+        long long cb = -1;
+        if (b < 0 && hm && j == 0) cb = claim_group(t, ep, v.G, status, &created);
+        cb = (long long)shfl64((unsigned long long)cb, half << 4);
+        created = __shfl_sync(kFull, (int)created, half << 4) != 0;
+        if (b < 0 && hm) {
+            b = cb;
+            if (created && j == 0) fresh = b;
+        }
     }
+    if (b >= 0) {
+        const size_t s = (size_t)b * kSlots + j;
+        if (created || v.pres != v.pres0)
+            t.keys[s] = v.pres ? ((v.G << kSlotBits) | (unsigned long long)j) : empty_key(j);
+        if (v.pres && v.dirty) store_amp<T>(t.amps, s, v.amp);
+        cnt_nnz += v.pres ? 1 : 0;
+        if (j == 0 && !hm) cnt_empty += 1;
+    }
+    return fresh;
+}
+
+// Append up to four new buckets (one candidate per half per held slot) to the live list.
+__device__ __forceinline__ void append_new(const TableDev& t, Ctl* ctl, long long fa, long long fb, int lane) {
+    const unsigned ma = __ballot_sync(kFull, fa >= 0), mb = __ballot_sync(kFull, fb >= 0);
+    const unsigned n = __popc(ma) + __popc(mb);
+    if (!n) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->list_tail, (unsigned long long)n);
+    base = shfl64(base, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (fa >= 0) t.list[base + __popc(ma & below)] = (unsigned)fa;
+    if (fb >= 0) t.list[base + __popc(ma) + __popc(mb & below)] = (unsigned)fb;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
@@ -140,21 +247,22 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// Block-reduce the pass counters and let the last block publish the pass: new epoch of the
-// output table, its key and group counts, the pass counter. Skipped when a pass failed.
-__device__ void finish_pass(Ctl* ctl, int p, unsigned ep_out, unsigned long long n, unsigned long long g,
-                            unsigned long long u, unsigned long long nnz_in, bool keys_fixed, unsigned amp_bytes) {
+// Block-reduce the pass counters; the last block to finish publishes the pass (key count,
+// list length, empty buckets, pass counter, amp updates, algorithmic bytes). Nothing is
+// published when a pass failed.
+__device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e, unsigned long long u,
+                            unsigned long long nnz_in, bool keys_fixed, unsigned amp_bytes) {
     __shared__ unsigned long long red[3][kThreads / 32];
     __shared__ bool last;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    n = warp_sum(n); g = warp_sum(g); u = warp_sum(u);
-    if (lane == 0) { red[0][w] = n; red[1][w] = g; red[2][w] = u; }
+    n = warp_sum(n); e = warp_sum(e); u = warp_sum(u);
+    if (lane == 0) { red[0][w] = n; red[1][w] = e; red[2][w] = u; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long bn = 0, bg = 0, bu = 0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { bn += red[0][i]; bg += red[1][i]; bu += red[2][i]; }
+        unsigned long long bn = 0, be = 0, bu = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { bn += red[0][i]; be += red[1][i]; bu += red[2][i]; }
         if (bn) atomicAdd(&ctl->acc_nnz, bn);
-        if (bg) atomicAdd(&ctl->acc_groups, bg);
+        if (be) atomicAdd(&ctl->acc_empty, be);
         if (bu) atomicAdd(&ctl->acc_upd, bu);
         __threadfence();
         const unsigned prev = atomicAdd(&ctl->done, 1u);
@@ -164,12 +272,12 @@ __device__ void finish_pass(Ctl* ctl, int p, unsigned ep_out, unsigned long long
     if (last && threadIdx.x == 0) {
         __threadfence();
         const unsigned long long tn = atomicExch(&ctl->acc_nnz, 0ULL);
-        const unsigned long long tg = atomicExch(&ctl->acc_groups, 0ULL);
+        const unsigned long long te = atomicExch(&ctl->acc_empty, 0ULL);
         const unsigned long long tu = atomicExch(&ctl->acc_upd, 0ULL);
         if (*(volatile unsigned int*)&ctl->status == 0) {
-            ctl->nnz[p ^ 1] = tn;
-            ctl->groups[p ^ 1] = tg;
-            ctl->epoch[p ^ 1] = ep_out;
+            ctl->nnz = tn;
+            ctl->empty_groups = te;
+            ctl->list_n = *(volatile unsigned long long*)&ctl->list_tail;
             ctl->amp_updates += tu;
             ctl->alg_bytes += keys_fixed ? nnz_in * (8ULL + 2ULL * amp_bytes) : (nnz_in + tn) * (8ULL + amp_bytes);
             ctl->seq += 1;
@@ -180,86 +288,92 @@ __device__ void finish_pass(Ctl* ctl, int p, unsigned ep_out, unsigned long long
 }
 
 template <class T, bool PAIR>
-__global__ void __launch_bounds__(kThreads, 4) pass_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kThreads, 3) pass_kernel(PassArgs a) {
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
-    const int p = (int)a.parity;
-    const unsigned ep_in = ctl->epoch[p];
-    const unsigned ep_out = ctl->epoch[p ^ 1] + 1;
-    const unsigned long long nnz_in = ctl->nnz[p];
-    const TableDev tin = p ? a.tab[1] : a.tab[0];
-    const TableDev tout = p ? a.tab[0] : a.tab[1];
-    const unsigned long long nb = tin.mask + 1;
+    const unsigned long long n = ctl->list_n;
+    if (PAIR && 2 * n > a.max_groups) {   // could overflow: refuse before touching the state
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
+        return;
+    }
+    const unsigned ep = ctl->epoch;
+    const unsigned long long nnz_in = ctl->nnz;
+    const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    unsigned long long cnt_nnz = 0, cnt_groups = 0, upd = 0;
+    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
+    Val<T> va, vb;
 
-    for (unsigned long long base = warp * 32; base < nb; base += nwarps * 32) {
-        const Header h = load_hdr(tin.hdr + base + lane);
-        unsigned vm = __ballot_sync(kFull, h.epoch == ep_in);
-        if (!PAIR) {
-            while (vm) {
-                const int i0 = __ffs(vm) - 1;
-                vm &= vm - 1;
-                int i1 = -1;
-                if (vm) { i1 = __ffs(vm) - 1; vm &= vm - 1; }
-                const int mi = half ? i1 : i0;
-                const bool act = mi >= 0;
-                const int src = act ? mi : i0;
-                unsigned long long G = shfl64(h.group, src);
-                const size_t s = (size_t)(base + src) * kSlots + j;
-                const unsigned long long key = act ? tin.keys[s] : 0ULL;
-                bool pres = act && (int)(key & 15ULL) == j;
-                Cx<T> amp = pres ? load_amp<T>(tin.amps, s) : czero<T>();
-                run_gates<T>(a.gates, a.g0, a.g1, false, G, lane, amp, pres, a.prune, upd);
-                write_group<T>(tout, ep_out, G, lane, act, amp, pres, &ctl->status, cnt_nnz, cnt_groups);
-            }
-        } else {
-            const uint32_t q = __ldg(&a.gates[a.g0].target);
-            const unsigned long long m = 1ULL << (q - kSlotBits);
-            while (vm) {
-                const int bi = __ffs(vm) - 1;
-                vm &= vm - 1;
-                const unsigned long long G = shfl64(h.group, bi);
+    if (!PAIR) {
+        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+            const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
+            const long long ba = ea < n ? (long long)t.list[ea] : -1;
+            const long long bb = eb < n ? (long long)t.list[eb] : -1;
+            const unsigned long long Ga = ba >= 0 ? load_hdr(t.hdr + ba).group : 0ULL;
+            const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
+            load_val<T>(t, va, Ga, ba, j);
+            load_val<T>(t, vb, Gb, bb, j);
+            run_gates<T>(a.gates, a.g0, a.g1, false, va, vb, lane, a.prune, upd);
+            write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+            write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        }
+    } else {
+        const uint32_t q = __ldg(&a.gates[a.g0].target);
+        const unsigned long long m = 1ULL << (q - kSlotBits);
+        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+            // lanes 0..3: one list entry each -> ownership and the pair's buckets
+            bool owner = false;
+            long long b0 = -1, b1 = -1;
+            unsigned long long G0 = 0;
+            if (lane < 4 && e0 + lane < n) {
+                const long long b = (long long)t.list[e0 + lane];
+                const unsigned long long G = load_hdr(t.hdr + b).group;
                 const bool mine1 = (G & m) != 0;
-                long long bp = -1;
-                if (lane == 0) bp = lookup_group(tin, ep_in, G ^ m);
-                bp = (long long)shfl64((unsigned long long)bp, 0);
-                if (mine1 && bp >= 0) continue;     // the bit-0 group owns this pair
-                const long long b = (long long)(base + bi);
-                const long long mb = half ? (mine1 ? b : bp) : (mine1 ? -1 : b);
-                unsigned long long Gh = half ? (G | m) : (G & ~m);
-                const size_t s = (size_t)(mb < 0 ? 0 : mb) * kSlots + j;
-                const unsigned long long key = mb >= 0 ? tin.keys[s] : 0ULL;
-                bool pres = mb >= 0 && (int)(key & 15ULL) == j;
-                Cx<T> amp = pres ? load_amp<T>(tin.amps, s) : czero<T>();
-                run_gates<T>(a.gates, a.g0, a.g1, true, Gh, lane, amp, pres, a.prune, upd);
-                write_group<T>(tout, ep_out, Gh, lane, true, amp, pres, &ctl->status, cnt_nnz, cnt_groups);
+                const long long bp = lookup_group(t, ep, G ^ m);
+                owner = !mine1 || bp < 0;
+                b0 = mine1 ? bp : b;
+                b1 = mine1 ? b : bp;
+                G0 = G & ~m;
+            }
+            unsigned om = __ballot_sync(kFull, owner) & 0xFu;
+            while (om) {
+                const int u0 = __ffs(om) - 1;
+                om &= om - 1;
+                int u1 = -1;
+                if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
+                const int u = half ? u1 : u0;
+                const int src = u >= 0 ? u : u0;
+                const long long ub0 = (long long)shfl64((unsigned long long)b0, src);
+                const long long ub1 = (long long)shfl64((unsigned long long)b1, src);
+                const unsigned long long uG0 = shfl64(G0, src);
+                const bool act = u >= 0;
+                load_val<T>(t, va, uG0, act ? ub0 : -1, j);
+                load_val<T>(t, vb, uG0 | m, act ? ub1 : -1, j);
+                run_gates<T>(a.gates, a.g0, a.g1, true, va, vb, lane, a.prune, upd);
+                const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+                const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+                append_new(t, ctl, fa, fb, lane);
             }
         }
     }
-    finish_pass(ctl, p, ep_out, cnt_nnz, cnt_groups, upd, nnz_in, a.keys_fixed != 0, a.amp_bytes);
+    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, a.amp_bytes);
 }
 
-// |0...0>: discard the state (both epochs advance past anything a failed pass may have
-// claimed), claim group 0 in table p and store key 0 with amplitude 1. One warp.
-__global__ void set_zero_kernel(TableDev t, Ctl* ctl, int p, int dbl) {
+// |0...0>: new epoch (every bucket becomes free), claim group 0, store key 0 with amplitude 1.
+__global__ void set_zero_kernel(TableDev t, Ctl* ctl, int dbl) {
     const int lane = threadIdx.x;
     __shared__ long long sb;
-    __shared__ unsigned sep;
     if (lane == 0) {
-        ctl->epoch[0] += 2;
-        ctl->epoch[1] += 2;
+        ctl->epoch += 1;
         ctl->status = 0;
         ctl->done = 0;
-        ctl->acc_nnz = ctl->acc_groups = ctl->acc_upd = 0;
+        ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
         ctl->seq = 0;
         ctl->amp_updates = 0;
         ctl->alg_bytes = 0;
-        const unsigned ep = ctl->epoch[p] + 1;
-        sep = ep;
-        sb = claim_group(t, ep, 0ULL, &ctl->status);
+        bool created;
+        sb = claim_group(t, ctl->epoch, 0ULL, &ctl->status, &created);
     }
     __syncwarp();
     const long long b = sb;
@@ -272,53 +386,56 @@ __global__ void set_zero_kernel(TableDev t, Ctl* ctl, int p, int dbl) {
         }
     }
     __syncwarp();
-    if (lane == 0 && b >= 0) {
-        ctl->epoch[p] = sep;
-        ctl->nnz[p] = 1;
-        ctl->groups[p] = 1;
-        ctl->nnz[p ^ 1] = 0;
-        ctl->groups[p ^ 1] = 0;
+    if (lane == 0) {
+        t.list[0] = (unsigned)(b >= 0 ? b : 0);
+        ctl->list_n = ctl->list_tail = b >= 0 ? 1 : 0;
+        ctl->nnz = b >= 0 ? 1 : 0;
+        ctl->empty_groups = 0;
     }
 }
 
-// set_state step 0: reset the control block and advance the epochs (one thread).
-__global__ void set_state_begin_kernel(Ctl* ctl, int p) {
-    ctl->epoch[0] += 2;
-    ctl->epoch[1] += 2;
-    ctl->epoch[p] += 1;
+// set_state step 0: new epoch, counters reset (one thread).
+__global__ void set_state_begin_kernel(Ctl* ctl) {
+    ctl->epoch += 1;
     ctl->status = 0;
     ctl->done = 0;
-    ctl->acc_nnz = ctl->acc_groups = ctl->acc_upd = 0;
+    ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
     ctl->seq = 0;
     ctl->amp_updates = 0;
     ctl->alg_bytes = 0;
     ctl->out_count = 0;
+    ctl->list_n = ctl->list_tail = 0;
+    ctl->nnz = 0;
+    ctl->empty_groups = 0;
 }
 
-// set_state step 1: claim the bucket of every entry's group (several entries may share one).
+// set_state step 1: claim the bucket of every entry's group; the claimer appends it to the list.
 __global__ void set_state_claim_kernel(const unsigned long long* __restrict__ keys, unsigned long long n,
-                                       TableDev t, Ctl* ctl, int p) {
-    const unsigned ep = ctl->epoch[p];
+                                       TableDev t, Ctl* ctl) {
+    const unsigned ep = ctl->epoch;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x)
-        claim_group(t, ep, keys[i] >> kSlotBits, &ctl->status);
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        bool created;
+        const long long b = claim_group(t, ep, keys[i] >> kSlotBits, &ctl->status, &created);
+        if (created) t.list[atomicAdd(&ctl->list_tail, 1ULL)] = (unsigned)b;
+    }
 }
 
-// set_state step 2: mark every slot of every live bucket empty.
-__global__ void set_state_clear_kernel(TableDev t, Ctl* ctl, int p) {
-    const unsigned ep = ctl->epoch[p];
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < nslots;
+// set_state step 2: mark every slot of every listed bucket empty.
+__global__ void set_state_clear_kernel(TableDev t, Ctl* ctl) {
+    const unsigned long long n = ctl->list_tail;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
-        if (load_hdr(t.hdr + (s >> kSlotBits)).epoch == ep) t.keys[s] = empty_key((int)(s & 15));
+        const unsigned b = t.list[s >> kSlotBits];
+        t.keys[(size_t)b * kSlots + (s & 15)] = empty_key((int)(s & 15));
     }
 }
 
 // set_state step 3: store every entry in its slot; a second store to a slot is a duplicate key.
 __global__ void set_state_fill_kernel(const unsigned long long* __restrict__ keys, const double* __restrict__ re,
                                       const double* __restrict__ im, unsigned long long n, TableDev t, Ctl* ctl,
-                                      int p, int dbl) {
-    const unsigned ep = ctl->epoch[p];
+                                      int dbl) {
+    const unsigned ep = ctl->epoch;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const unsigned long long k = keys[i];
@@ -333,66 +450,70 @@ __global__ void set_state_fill_kernel(const unsigned long long* __restrict__ key
     }
 }
 
-// Count live buckets and present keys of table p into ctl->nnz[p] / groups[p] (adds; the
-// host zeroes them first).
-__global__ void count_kernel(TableDev t, Ctl* ctl, int p) {
-    const unsigned ep = ctl->epoch[p];
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
-    unsigned long long n = 0, g = 0;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < nslots;
-         s += (unsigned long long)gridDim.x * blockDim.x) {
-        if (load_hdr(t.hdr + (s >> kSlotBits)).epoch != ep) continue;
+// set_state step 4 (one thread): commit the list.
+__global__ void set_state_end_kernel(Ctl* ctl, unsigned long long n) {
+    ctl->list_n = ctl->list_tail;
+    ctl->nnz = n;
+}
+
+// Present keys and empty live buckets over the list, into ctl->acc_nnz / acc_empty (adds).
+__global__ void count_kernel(TableDev t, Ctl* ctl) {
+    const unsigned long long n = ctl->list_n;
+    unsigned long long c = 0, e = 0;
+    for (unsigned long long s0 = (unsigned long long)blockIdx.x * blockDim.x; s0 < n * kSlots;
+         s0 += (unsigned long long)gridDim.x * blockDim.x) {   // same trip count for the whole block
+        const unsigned long long s = s0 + threadIdx.x;
         const int j = (int)(s & 15);
-        n += (int)(t.keys[s] & 15ULL) == j;
-        g += j == 0;
+        bool p = false;
+        if (s < n * kSlots) p = slot_present(t.keys[(size_t)t.list[s >> kSlotBits] * kSlots + j], j);
+        c += p;
+        const unsigned grp = __ballot_sync(kFull, p);
+        if (s < n * kSlots && j == 0 && ((grp >> (threadIdx.x & 16)) & 0xFFFFu) == 0) e += 1;
     }
-    n = warp_sum(n);
-    g = warp_sum(g);
+    c = warp_sum(c);
+    e = warp_sum(e);
     if ((threadIdx.x & 31) == 0) {
-        if (n) atomicAdd(&ctl->nnz[p], n);
-        if (g) atomicAdd(&ctl->groups[p], g);
+        if (c) atomicAdd(&ctl->acc_nnz, c);
+        if (e) atomicAdd(&ctl->acc_empty, e);
     }
 }
 
-// Compact the present entries of table p into (keys, re, im). Each warp owns a contiguous
-// range of buckets: it counts, reserves its span with one atomic, then writes. Entries
-// beyond cap are counted but not written.
+// Compact the present entries into (keys ^ frame, re, im). Each warp owns a contiguous range
+// of list entries: it counts, reserves its span with one atomic, then writes. Entries beyond
+// cap are counted but not written.
 template <class T>
-__global__ void readout_kernel(TableDev t, Ctl* ctl, int p, unsigned long long* okeys, double* ore,
-                               double* oim, unsigned long long cap, int drop_negl, PruneBits pb,
+__global__ void readout_kernel(TableDev t, Ctl* ctl, unsigned long long frame, unsigned long long* okeys,
+                               double* ore, double* oim, unsigned long long cap, int drop_negl, PruneBits pb,
                                unsigned long long range) {
-    const unsigned ep = ctl->epoch[p];
-    const unsigned long long nb = t.mask + 1;
+    const unsigned long long n = ctl->list_n;
     const int lane = threadIdx.x & 31, j = lane & 15, half = lane >> 4;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long r0 = warp * range; r0 < nb; r0 += nwarps * range) {
-        const unsigned long long r1 = r0 + range < nb ? r0 + range : nb;
+    for (unsigned long long r0 = warp * range; r0 < n; r0 += nwarps * range) {
+        const unsigned long long r1 = r0 + range < n ? r0 + range : n;
         unsigned long long cnt = 0;
-        for (unsigned long long bb = r0; bb < r1; bb += 2) {   // same trip count in both halves
-            const unsigned long long b = bb + half;
+        for (unsigned long long ee = r0; ee < r1; ee += 2) {   // same trip count in both halves
+            const unsigned long long e = ee + half;
             bool keep = false;
-            if (b < r1 && load_hdr(t.hdr + b).epoch == ep) {
-                const size_t s = (size_t)b * kSlots + j;
-                keep = (int)(t.keys[s] & 15ULL) == j;
+            if (e < r1) {
+                const size_t s = (size_t)t.list[e] * kSlots + j;
+                keep = slot_present(t.keys[s], j);
                 if (keep && drop_negl) keep = !negligible(load_amp<T>(t.amps, s), pb);
             }
             cnt += __popc(__ballot_sync(kFull, keep));
         }
-        // every lane holds the same total (each ballot is warp-wide); both halves counted
-        cnt = __shfl_sync(kFull, cnt, 0);
         unsigned long long base = 0;
         if (lane == 0 && cnt) base = atomicAdd(&ctl->out_count, cnt);
-        base = __shfl_sync(kFull, base, 0);
+        base = shfl64(base, 0);
         if (!cnt) continue;
         unsigned long long pos = base;
-        for (unsigned long long bb = r0; bb < r1; bb += 2) {
-            const unsigned long long b = bb + half;
+        for (unsigned long long ee = r0; ee < r1; ee += 2) {
+            const unsigned long long e = ee + half;
             bool keep = false;
             size_t s = 0;
-            if (b < r1 && load_hdr(t.hdr + b).epoch == ep) {
-                s = (size_t)b * kSlots + j;
-                keep = (int)(t.keys[s] & 15ULL) == j;
+            if (e < r1) {
+                s = (size_t)t.list[e] * kSlots + j;
+                keep = slot_present(t.keys[s], j);
                 if (keep && drop_negl) keep = !negligible(load_amp<T>(t.amps, s), pb);
             }
             const unsigned bal = __ballot_sync(kFull, keep);
@@ -400,7 +521,7 @@ __global__ void readout_kernel(TableDev t, Ctl* ctl, int p, unsigned long long* 
                 const unsigned long long at = pos + __popc(bal & ((1u << lane) - 1u));
                 if (at < cap) {
                     const Cx<T> v = load_amp<T>(t.amps, s);
-                    okeys[at] = t.keys[s];
+                    okeys[at] = t.keys[s] ^ frame;
                     ore[at] = (double)v.r;
                     oim[at] = (double)v.i;
                 }
@@ -410,17 +531,16 @@ __global__ void readout_kernel(TableDev t, Ctl* ctl, int p, unsigned long long* 
     }
 }
 
-// Sum of |a|^2 over table p, accumulated in FP64, into ctl->acc[0].
+// Sum of |a|^2 over the state, accumulated in FP64, into ctl->acc[0].
 template <class T>
-__global__ void norm_kernel(TableDev t, Ctl* ctl, int p) {
-    const unsigned ep = ctl->epoch[p];
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
+__global__ void norm_kernel(TableDev t, Ctl* ctl) {
+    const unsigned long long n = ctl->list_n;
     double acc = 0.0;
-    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < nslots;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
-        if (load_hdr(t.hdr + (s >> kSlotBits)).epoch != ep) continue;
-        if ((int)(t.keys[s] & 15ULL) != (int)(s & 15)) continue;
-        const Cx<T> v = load_amp<T>(t.amps, s);
+        const size_t slot = (size_t)t.list[s >> kSlotBits] * kSlots + (s & 15);
+        if (!slot_present(t.keys[slot], (int)(s & 15))) continue;
+        const Cx<T> v = load_amp<T>(t.amps, slot);
         const double r = (double)v.r, i = (double)v.i;
         acc = __fma_rn(r, r, __fma_rn(i, i, acc));
     }
@@ -432,30 +552,33 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double 
     atomicMax(p, (unsigned long long)__double_as_longlong(v));
 }
 
-// Overlap of state a with state b over the keys of a: acc[0..1] += conj(b)*a, acc[2] += |a|^2,
-// acc[3] += |b|^2 (keys of a), max |a-b|. One warp per bucket of a (half-warps alternate).
-__global__ void compare_a_kernel(TableDev ta, unsigned ep_a, int dbl_a, TableDev tb, unsigned ep_b, int dbl_b,
-                                 Ctl* out) {
-    const unsigned long long nb = ta.mask + 1;
-    const int lane = threadIdx.x & 31, j = lane & 15, half = lane >> 4;
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+// Amplitude of the key stored as sb in state B, if present.
+__device__ __forceinline__ bool find_other(const TableDev& tb, unsigned ep_b, unsigned long long sb, bool dbl_b,
+                                           Cx<double>* out) {
+    const long long bb = lookup_group(tb, ep_b, sb >> kSlotBits);
+    if (bb < 0) return false;
+    const int j = (int)(sb & 15ULL);
+    const size_t s = (size_t)bb * kSlots + j;
+    if (!slot_present(tb.keys[s], j)) return false;
+    *out = load_amp_any(tb.amps, s, dbl_b);
+    return true;
+}
+
+// Over the keys of a: acc[0..1] += conj(b)*a, acc[2] += |a|^2, acc[3] += |b|^2, max |a-b|.
+// d = frame_a ^ frame_b translates a stored key of a into b's frame.
+__global__ void compare_a_kernel(TableDev ta, const Ctl* ca, int dbl_a, TableDev tb, const Ctl* cb, int dbl_b,
+                                 unsigned long long d, Ctl* out) {
+    const unsigned long long n = ca->list_n;
+    const unsigned ep_b = cb->epoch;
     double ore = 0, oim = 0, na = 0, nbb = 0, mx = 0;
-    for (unsigned long long b0 = warp * 2; b0 < nb; b0 += nwarps * 2) {
-        const unsigned long long b = b0 + half;
-        const bool live = b < nb && load_hdr(ta.hdr + b).epoch == ep_a;
-        long long bb = -1;
-        if (live && j == 0) bb = lookup_group(tb, ep_b, load_hdr(ta.hdr + b).group);
-        bb = (long long)shfl64((unsigned long long)bb, half << 4);
-        if (!live) continue;
-        const size_t s = (size_t)b * kSlots + j;
-        if ((int)(ta.keys[s] & 15ULL) != j) continue;
-        const Cx<double> va = load_amp_any(ta.amps, s, dbl_a);
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const size_t slot = (size_t)ta.list[s >> kSlotBits] * kSlots + (s & 15);
+        const unsigned long long key = ta.keys[slot];
+        if (!slot_present(key, (int)(s & 15))) continue;
+        const Cx<double> va = load_amp_any(ta.amps, slot, dbl_a);
         Cx<double> vb{0.0, 0.0};
-        if (bb >= 0) {
-            const size_t sb = (size_t)bb * kSlots + j;
-            if ((int)(tb.keys[sb] & 15ULL) == j) vb = load_amp_any(tb.amps, sb, dbl_b);
-        }
+        find_other(tb, ep_b, key ^ d, dbl_b, &vb);
         ore += vb.r * va.r + vb.i * va.i;
         oim += vb.r * va.i - vb.i * va.r;
         na += va.r * va.r + va.i * va.i;
@@ -465,7 +588,7 @@ __global__ void compare_a_kernel(TableDev ta, unsigned ep_a, int dbl_a, TableDev
     }
     ore = warp_sum(ore); oim = warp_sum(oim); na = warp_sum(na); nbb = warp_sum(nbb);
     for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(kFull, mx, o));
-    if (lane == 0) {
+    if ((threadIdx.x & 31) == 0) {
         atomicAdd(&out->acc[0], ore);
         atomicAdd(&out->acc[1], oim);
         atomicAdd(&out->acc[2], na);
@@ -475,58 +598,65 @@ __global__ void compare_a_kernel(TableDev ta, unsigned ep_a, int dbl_a, TableDev
 }
 
 // Keys of b absent from a: acc[4] += |b|^2, max |b|.
-__global__ void compare_b_kernel(TableDev ta, unsigned ep_a, TableDev tb, unsigned ep_b, int dbl_b, Ctl* out) {
-    const unsigned long long nb = tb.mask + 1;
-    const int lane = threadIdx.x & 31, j = lane & 15, half = lane >> 4;
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+__global__ void compare_b_kernel(TableDev ta, const Ctl* ca, TableDev tb, const Ctl* cb, int dbl_b,
+                                 unsigned long long d, Ctl* out) {
+    const unsigned long long n = cb->list_n;
+    const unsigned ep_a = ca->epoch;
     double nbo = 0, mx = 0;
-    for (unsigned long long b0 = warp * 2; b0 < nb; b0 += nwarps * 2) {
-        const unsigned long long b = b0 + half;
-        const bool live = b < nb && load_hdr(tb.hdr + b).epoch == ep_b;
-        long long ba = -1;
-        if (live && j == 0) ba = lookup_group(ta, ep_a, load_hdr(tb.hdr + b).group);
-        ba = (long long)shfl64((unsigned long long)ba, half << 4);
-        if (!live) continue;
-        const size_t s = (size_t)b * kSlots + j;
-        if ((int)(tb.keys[s] & 15ULL) != j) continue;
-        bool in_a = false;
-        if (ba >= 0) in_a = (int)(ta.keys[(size_t)ba * kSlots + j] & 15ULL) == j;
-        if (in_a) continue;
-        const Cx<double> vb = load_amp_any(tb.amps, s, dbl_b);
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const size_t slot = (size_t)tb.list[s >> kSlotBits] * kSlots + (s & 15);
+        const unsigned long long key = tb.keys[slot];
+        if (!slot_present(key, (int)(s & 15))) continue;
+        Cx<double> dummy;
+        if (find_other(ta, ep_a, key ^ d, true, &dummy)) continue;
+        const Cx<double> vb = load_amp_any(tb.amps, slot, dbl_b);
         nbo += vb.r * vb.r + vb.i * vb.i;
         mx = fmax(mx, sqrt(vb.r * vb.r + vb.i * vb.i));
     }
     nbo = warp_sum(nbo);
     for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(kFull, mx, o));
-    if (lane == 0) {
+    if ((threadIdx.x & 31) == 0) {
         atomicAdd(&out->acc[4], nbo);
         atomic_max_nonneg(&out->acc_max, mx);
     }
 }
 
-// Move the content of an old table into a larger new one (fresh headers, epoch ep_new).
-// Every group appears once in the old table, so each new bucket has one writer.
-__global__ void rehash_kernel(TableDev told, unsigned ep_old, TableDev tnew, unsigned ep_new, int amp_bytes,
-                              Ctl* ctl) {
-    const unsigned long long nb = told.mask + 1;
+// Copy the live, non-empty buckets of the old table into a new one (fresh headers, epoch
+// ep_new), rebuilding the list. Each group appears once, so each new bucket has one writer.
+__global__ void rehash_kernel(TableDev told, unsigned long long n_old, TableDev tnew, unsigned ep_new,
+                              int amp_bytes, Ctl* ctl) {
     const int lane = threadIdx.x & 31, j = lane & 15, half = lane >> 4;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long b0 = warp * 2; b0 < nb; b0 += nwarps * 2) {
-        const unsigned long long b = b0 + half;
-        const Header h = b < nb ? load_hdr(told.hdr + b) : Header{0, 0, 0};
-        const bool live = b < nb && h.epoch == ep_old;
+    for (unsigned long long e0 = warp * 2; e0 < n_old; e0 += nwarps * 2) {
+        const unsigned long long e = e0 + half;
+        const bool in = e < n_old;
+        const unsigned b = in ? told.list[e] : 0u;
+        const size_t s = (size_t)b * kSlots + j;
+        const unsigned long long k = in ? told.keys[s] : 0ULL;
+        const bool p = in && slot_present(k, j);
+        const unsigned bal = __ballot_sync(kFull, p);
+        const bool keep = in && ((half ? (bal >> 16) : (bal & 0xFFFFu)) != 0);
         long long nbk = -1;
-        if (live && j == 0) nbk = claim_group(tnew, ep_new, h.group, &ctl->status);
+        bool created = false;
+        if (keep && j == 0) nbk = claim_group(tnew, ep_new, load_hdr(told.hdr + b).group, &ctl->status, &created);
         nbk = (long long)shfl64((unsigned long long)nbk, half << 4);
-        if (!live || nbk < 0) continue;
-        const size_t s = (size_t)b * kSlots + j, d = (size_t)nbk * kSlots + j;
-        const unsigned long long k = told.keys[s];
-        tnew.keys[d] = k;
-        if ((int)(k & 15ULL) == j) {
-            if (amp_bytes == 16) reinterpret_cast<double2*>(tnew.amps)[d] = reinterpret_cast<const double2*>(told.amps)[s];
-            else reinterpret_cast<float2*>(tnew.amps)[d] = reinterpret_cast<const float2*>(told.amps)[s];
+        const long long fresh = (keep && j == 0 && nbk >= 0) ? nbk : -1;
+        if (keep && nbk >= 0) {
+            const size_t d = (size_t)nbk * kSlots + j;
+            tnew.keys[d] = k;
+            if (p) {
+                if (amp_bytes == 16) reinterpret_cast<double2*>(tnew.amps)[d] = reinterpret_cast<const double2*>(told.amps)[s];
+                else reinterpret_cast<float2*>(tnew.amps)[d] = reinterpret_cast<const float2*>(told.amps)[s];
+            }
+        }
+        const unsigned fm = __ballot_sync(kFull, fresh >= 0);
+        if (fm) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&ctl->list_tail, (unsigned long long)__popc(fm));
+            base = shfl64(base, 0);
+            if (fresh >= 0) tnew.list[base + __popc(fm & ((1u << lane) - 1u))] = (unsigned)fresh;
         }
     }
 }
@@ -541,9 +671,28 @@ int grid_for(unsigned long long work_items, int per_block, int sms) {
 
 }  // namespace
 
-cudaError_t launch_pass(const PassArgs& a, bool dbl, int sms, cudaStream_t st) {
-    const unsigned long long nb = a.tab[a.parity].mask + 1;
-    const int grid = grid_for(nb / 32 + 1, kThreads / 32, sms);
+// Resident blocks per SM of each pass-kernel instantiation (queried once per process).
+int pass_residency(bool dbl, bool pair) {
+    static int cache[4] = {0, 0, 0, 0};
+    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
+    if (!c) {
+        int n = 0;
+        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<double, true>, kThreads, 0);
+        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<double, false>, kThreads, 0);
+        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<float, true>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<float, false>, kThreads, 0);
+        c = n > 0 ? n : 1;
+    }
+    return c;
+}
+
+cudaError_t launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
+    // list_hint bounds the live-bucket count; the grid is sized from it (a warp takes four
+    // list entries per step) and capped at one resident wave; the kernel reads the exact
+    // count on the device.
+    unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
+    const unsigned long long wave = (unsigned long long)sms * pass_residency(dbl, a.pair != 0);
+    const int grid = (int)std::max<unsigned long long>(1, std::min(g, wave));
     if (dbl) {
         if (a.pair) pass_kernel<double, true><<<grid, kThreads, 0, st>>>(a);
         else pass_kernel<double, false><<<grid, kThreads, 0, st>>>(a);
@@ -554,63 +703,59 @@ cudaError_t launch_pass(const PassArgs& a, bool dbl, int sms, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, int p, bool dbl, cudaStream_t st) {
-    set_zero_kernel<<<1, 32, 0, st>>>(t, ctl, p, dbl ? 1 : 0);
+cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st) {
+    set_zero_kernel<<<1, 32, 0, st>>>(t, ctl, dbl ? 1 : 0);
     return cudaGetLastError();
 }
 
 cudaError_t launch_set_state(const unsigned long long* keys, const double* re, const double* im,
-                             unsigned long long n, const TableDev& t, Ctl* ctl, int p, bool dbl, int sms,
+                             unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,
                              cudaStream_t st) {
-    set_state_begin_kernel<<<1, 1, 0, st>>>(ctl, p);
+    set_state_begin_kernel<<<1, 1, 0, st>>>(ctl);
     const int ge = grid_for(n, kThreads, sms);
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
-    const int gs = grid_for(nslots, kThreads, sms);
-    if (n) set_state_claim_kernel<<<ge, kThreads, 0, st>>>(keys, n, t, ctl, p);
-    set_state_clear_kernel<<<gs, kThreads, 0, st>>>(t, ctl, p);
-    if (n) set_state_fill_kernel<<<ge, kThreads, 0, st>>>(keys, re, im, n, t, ctl, p, dbl ? 1 : 0);
-    count_kernel<<<gs, kThreads, 0, st>>>(t, ctl, p);
+    if (n) {
+        set_state_claim_kernel<<<ge, kThreads, 0, st>>>(keys, n, t, ctl);
+        set_state_clear_kernel<<<grid_for(n * kSlots, kThreads, sms), kThreads, 0, st>>>(t, ctl);
+        set_state_fill_kernel<<<ge, kThreads, 0, st>>>(keys, re, im, n, t, ctl, dbl ? 1 : 0);
+    }
+    set_state_end_kernel<<<1, 1, 0, st>>>(ctl, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_count(const TableDev& t, Ctl* ctl, int p, int sms, cudaStream_t st) {
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
-    count_kernel<<<grid_for(nslots, kThreads, sms), kThreads, 0, st>>>(t, ctl, p);
+cudaError_t launch_count(const TableDev& t, Ctl* ctl, unsigned long long list_hint, int sms, cudaStream_t st) {
+    count_kernel<<<grid_for(list_hint * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(t, ctl);
     return cudaGetLastError();
 }
 
-cudaError_t launch_readout(const TableDev& t, Ctl* ctl, int p, bool dbl, unsigned long long* okeys, double* ore,
-                           double* oim, unsigned long long cap, bool drop_negl, PruneBits pb, int sms,
-                           cudaStream_t st) {
-    const unsigned long long nb = t.mask + 1;
-    const unsigned long long range = 256;
-    const int grid = grid_for((nb + range - 1) / range, kThreads / 32, sms);
-    if (dbl) readout_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, p, okeys, ore, oim, cap, drop_negl, pb, range);
-    else readout_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, p, okeys, ore, oim, cap, drop_negl, pb, range);
+cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_hint, unsigned long long frame,
+                           bool dbl, unsigned long long* okeys, double* ore, double* oim, unsigned long long cap,
+                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st) {
+    const unsigned long long range = 64;
+    const int grid = grid_for((list_hint + range - 1) / range + 1, kThreads / 32, sms);
+    if (dbl) readout_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range);
+    else readout_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range);
     return cudaGetLastError();
 }
 
-cudaError_t launch_norm(const TableDev& t, Ctl* ctl, int p, bool dbl, int sms, cudaStream_t st) {
-    const unsigned long long nslots = (t.mask + 1) * kSlots;
-    const int grid = grid_for(nslots, kThreads, sms);
-    if (dbl) norm_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, p);
-    else norm_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, p);
+cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
+    const int grid = grid_for(list_hint * kSlots + 1, kThreads, sms);
+    if (dbl) norm_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl);
+    else norm_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl);
     return cudaGetLastError();
 }
 
-cudaError_t launch_compare(const TableDev& ta, unsigned ep_a, bool dbl_a, const TableDev& tb, unsigned ep_b,
-                           bool dbl_b, Ctl* out, int sms, cudaStream_t st) {
-    const int ga = grid_for((ta.mask + 1) / 2 + 1, kThreads / 32, sms);
-    const int gb = grid_for((tb.mask + 1) / 2 + 1, kThreads / 32, sms);
-    compare_a_kernel<<<ga, kThreads, 0, st>>>(ta, ep_a, dbl_a, tb, ep_b, dbl_b, out);
-    compare_b_kernel<<<gb, kThreads, 0, st>>>(ta, ep_a, tb, ep_b, dbl_b, out);
+cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,
+                           const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
+                           unsigned long long d, Ctl* out, int sms, cudaStream_t st) {
+    compare_a_kernel<<<grid_for(hint_a * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(ta, ca, dbl_a, tb, cb, dbl_b, d, out);
+    compare_b_kernel<<<grid_for(hint_b * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(ta, ca, tb, cb, dbl_b, d, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_rehash(const TableDev& told, unsigned ep_old, const TableDev& tnew, unsigned ep_new,
+cudaError_t launch_rehash(const TableDev& told, unsigned long long n_old, const TableDev& tnew, unsigned ep_new,
                           int amp_bytes, Ctl* ctl, int sms, cudaStream_t st) {
-    const int grid = grid_for((told.mask + 1) / 2 + 1, kThreads / 32, sms);
-    rehash_kernel<<<grid, kThreads, 0, st>>>(told, ep_old, tnew, ep_new, amp_bytes, ctl);
+    const int grid = grid_for(n_old / 2 + 1, kThreads / 32, sms);
+    rehash_kernel<<<grid, kThreads, 0, st>>>(told, n_old, tnew, ep_new, amp_bytes, ctl);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,6 @@
 // Host-side launchers of the engine's kernels. Every launcher enqueues on the given stream
-// and returns the launch status; none synchronizes.
+// and returns the launch status; none synchronizes. list_hint is an upper bound on the
+// state's live-bucket count, used only to size grids (the kernels read the exact count).
 #pragma once
 #include <cuda_runtime_api.h>
 #include "sqc_types.h"
@@ -9,19 +10,21 @@
 
 namespace sqc {
 
-cudaError_t launch_pass(const PassArgs& a, bool dbl, int sms, cudaStream_t st);
-cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, int p, bool dbl, cudaStream_t st);
+cudaError_t launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st);
+cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st);
 cudaError_t launch_set_state(const unsigned long long* keys, const double* re, const double* im,
-                             unsigned long long n, const TableDev& t, Ctl* ctl, int p, bool dbl, int sms,
+                             unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,
                              cudaStream_t st);
-cudaError_t launch_count(const TableDev& t, Ctl* ctl, int p, int sms, cudaStream_t st);
-cudaError_t launch_readout(const TableDev& t, Ctl* ctl, int p, bool dbl, unsigned long long* okeys, double* ore,
-                           double* oim, unsigned long long cap, bool drop_negl, PruneBits pb, int sms,
-                           cudaStream_t st);
-cudaError_t launch_norm(const TableDev& t, Ctl* ctl, int p, bool dbl, int sms, cudaStream_t st);
-cudaError_t launch_compare(const TableDev& ta, unsigned ep_a, bool dbl_a, const TableDev& tb, unsigned ep_b,
-                           bool dbl_b, Ctl* out, int sms, cudaStream_t st);
-cudaError_t launch_rehash(const TableDev& told, unsigned ep_old, const TableDev& tnew, unsigned ep_new,
+cudaError_t launch_count(const TableDev& t, Ctl* ctl, unsigned long long list_hint, int sms, cudaStream_t st);
+cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_hint, unsigned long long frame,
+                           bool dbl, unsigned long long* okeys, double* ore, double* oim, unsigned long long cap,
+                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st);
+cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, int sms,
+                        cudaStream_t st);
+cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,
+                           const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
+                           unsigned long long d, Ctl* out, int sms, cudaStream_t st);
+cudaError_t launch_rehash(const TableDev& told, unsigned long long n_old, const TableDev& tnew, unsigned ep_new,
                           int amp_bytes, Ctl* ctl, int sms, cudaStream_t st);
 
 }  // namespace sqc
