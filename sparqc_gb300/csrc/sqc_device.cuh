@@ -265,4 +265,21 @@ __device__ __forceinline__ bool negligible(Cx<float> v, const PruneBits& t) {
     return ((unsigned)__float_as_int(v.r) & 0x7FFFFFFFu) <= t.f && ((unsigned)__float_as_int(v.i) & 0x7FFFFFFFu) <= t.f;
 }
 
+// ---- asynchronous global -> shared copies (sm_80+ PTX) ----------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Asynchronous 16-byte global -> shared copy (both addresses 16-byte aligned), L2 only.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+// Close the thread's current group of cp.async copies.
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Wait until at most N of the thread's committed cp.async groups are still in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 }  // namespace sqc

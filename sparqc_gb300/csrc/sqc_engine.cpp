@@ -61,7 +61,8 @@ int Engine::cuda(cudaError_t e, const char* what) {
 }
 
 size_t Engine::bucket_bytes() const {
-    return sizeof(Header) + kSlots * sizeof(unsigned long long) + kSlots * (dbl_ ? 16 : 8) + sizeof(unsigned);
+    return sizeof(Header) + kSlots * sizeof(unsigned long long) + kSlots * (dbl_ ? 16 : 8) + sizeof(unsigned) +
+           sizeof(Unit);
 }
 
 unsigned long long Engine::max_groups() const { return (unsigned long long)(kMaxLoad * (double)tab_.nb); }
@@ -130,6 +131,8 @@ int Engine::alloc_table(unsigned long long nb, HostTable* out) {
         (rc = cuda(cudaMalloc(&t.keys, nb * kSlots * sizeof(unsigned long long)), "cudaMalloc(keys)")) ||
         (rc = cuda(cudaMalloc(&t.amps, nb * kSlots * (dbl_ ? 16 : 8)), "cudaMalloc(amps)")) ||
         (rc = cuda(cudaMalloc(&t.list, nb * sizeof(unsigned)), "cudaMalloc(list)")) ||
+        (rc = cuda(cudaMalloc(&t.units, nb * sizeof(Unit)), "cudaMalloc(units)")) ||
+        (rc = cuda(cudaMalloc(&t.counts, (nb / 32 + 1) * sizeof(unsigned)), "cudaMalloc(counts)")) ||
         (rc = cuda(cudaMemsetAsync(t.hdr, 0, nb * sizeof(Header), stream_), "cudaMemset(hdr)"))) {
         free_table(&t);
         return rc;
@@ -143,6 +146,8 @@ void Engine::free_table(HostTable* t) {
     if (t->keys) cudaFree(t->keys);
     if (t->amps) cudaFree(t->amps);
     if (t->list) cudaFree(t->list);
+    if (t->units) cudaFree(t->units);
+    if (t->counts) cudaFree(t->counts);
     *t = HostTable();
 }
 
@@ -152,6 +157,8 @@ TableDev Engine::dev() const {
     d.keys = tab_.keys;
     d.amps = tab_.amps;
     d.list = tab_.list;
+    d.units = tab_.units;
+    d.counts = tab_.counts;
     d.mask = tab_.nb - 1;
     return d;
 }
@@ -388,11 +395,13 @@ int Engine::flush() {
         a.pair = pair ? 1u : 0u;
         a.keys_fixed = fixed ? 1u : 0u;
         if (pair) list_hint_ = std::min<unsigned long long>(tab_.nb, 2 * list_hint_);
-        if ((rc = cuda(launch_pass(a, list_hint_, dbl_, sms_, stream_), "gate pass"))) return rc;
+        a.range = pass_range(list_hint_, sms_);
+        const int nl = launch_pass(a, list_hint_, dbl_, sms_, stream_);
+        if (nl < 0) return cuda(cudaGetLastError(), "gate pass");
         passes_.push_back(PassRec{snap_log_, snap_plan_});
         snap_log_ = src[i - 1] + 1;
         snap_plan_ = after[i - 1];
-        ++launches_;
+        launches_ += (uint64_t)nl;
         ++passes_run_;
     }
     desc_used_ += nd;
@@ -459,7 +468,9 @@ int Engine::rebuild(unsigned long long nb_new) {
     if ((rc = cuda(cudaMemcpyAsync(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice, stream_), "H2D ctl")))
         return rc;
     TableDev nd;
-    nd.hdr = nt.hdr; nd.keys = nt.keys; nd.amps = nt.amps; nd.list = nt.list; nd.mask = nt.nb - 1;
+    nd.hdr = nt.hdr; nd.keys = nt.keys; nd.amps = nt.amps; nd.list = nt.list; nd.units = nt.units;
+    nd.counts = nt.counts;
+    nd.mask = nt.nb - 1;
     if ((rc = cuda(launch_rehash(dev(), n_old, nd, 1u, dbl_ ? 16 : 8, ctl_, sms_, stream_), "rehash"))) return rc;
     ++launches_;
     if ((rc = read_ctl())) return rc;

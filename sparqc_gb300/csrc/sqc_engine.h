@@ -18,6 +18,8 @@ struct HostTable {
     unsigned long long* keys = nullptr;
     void* amps = nullptr;
     unsigned int* list = nullptr;
+    Unit* units = nullptr;
+    unsigned int* counts = nullptr;
     unsigned long long nb = 0;
 };
 

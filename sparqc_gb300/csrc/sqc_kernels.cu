@@ -1,23 +1,6 @@
-// Gate-pass and bookkeeping kernels of the sparse statevector engine (sm_103a).
-//
-// A gate pass updates the table in place; it walks the list of live buckets.
-//  * stream pass: a run of gates that never pair keys across 16-key groups -- diagonal gates
-//    on any qubit and any gate on qubits 0..3 (the partner sits in the same bucket and is
-//    reached with a warp shuffle). Each half-warp streams two buckets (lane j holds slot j of
-//    both), so a warp keeps four buckets in flight.
-//  * pair pass: a gate whose partner key lives in another group (branching gate on a qubit
-//    >= 4, or X/Y on a qubit >= 4 with controls the host could not resolve), followed by a
-//    stream run. A half-warp takes the group pair (G0, G1 = G0 | m): lane j holds slot j of
-//    both groups, so the pair update is lane-local. The group with stored target bit 0 owns
-//    the pair; the other owns it only when its partner group is absent -- the reference's pair
-//    rule (emulator/device/device_table_FC.cuh:62-110) lifted from keys to 16-key groups,
-//    which gives the same pairs and the same per-key results. Ownership lookups of four list
-//    entries run in parallel; owned pairs are packed two per warp.
-// Every pair with at least one present member is read once and written back once, at the
-// same place. A group that appears for the first time is claimed with a 128-bit CAS and
-// appended to the list; such groups are not revisited in the same pass. Pruning follows the
-// reference (emulator/device/device_data.cuh:108-156): branching gates drop negligible
-// outputs, swap and diagonal gates keep every key.
+// Bookkeeping kernels of the sparse statevector engine (sm_103a): reset, loading a state,
+// counting, readout, norm, state comparison and table rebuild. All walk the list of live
+// buckets. The gate passes are in sqc_pass.cu.
 #include "sqc_kernels.h"
 
 #include <algorithm>
@@ -52,192 +35,6 @@ template <class T> __device__ __forceinline__ Cx<T> czero() { return Cx<T>{T(0),
 
 __device__ __forceinline__ bool slot_present(unsigned long long key, int j) { return (int)(key & 15ULL) == j; }
 
-// One slot held by a lane: its group, amplitude and presence, where it lives (b = -1 for a
-// group absent at the start of the pass) and whether the pass changed it.
-template <class T> struct Val {
-    unsigned long long G;
-    long long b;
-    Cx<T> amp;
-    bool pres, pres0, dirty;
-};
-
-template <class T>
-__device__ __forceinline__ void load_val(const TableDev& t, Val<T>& v, unsigned long long G, long long b, int j) {
-    v.G = G;
-    v.b = b;
-    v.dirty = false;
-    v.pres = false;
-    v.amp = czero<T>();
-    if (b >= 0) {
-        const size_t s = (size_t)b * kSlots + j;
-        v.pres = slot_present(t.keys[s], j);
-        if (v.pres) v.amp = load_amp<T>(t.amps, s);
-    }
-    v.pres0 = v.pres;
-}
-
-struct GateHead {
-    uint32_t kind, target, flip, credit;
-    unsigned long long ctrl, cval;
-};
-
-__device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
-    GateHead h;
-    h.kind = __ldg(&g->kind);
-    h.target = __ldg(&g->target);
-    h.flip = __ldg(&g->flip);
-    h.credit = __ldg(&g->pad);
-    h.ctrl = __ldg(&g->ctrl);
-    h.cval = __ldg(&g->cval);
-    return h;
-}
-
-// One streamable gate on one held slot. `off` is the lane distance to the partner slot
-// (1 << q for q < 4, inside the half-warp) or 0 for a diagonal gate on a qubit >= 4.
-template <class T>
-__device__ __forceinline__ void gate_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
-                                          const PruneBits& pb) {
-    const unsigned long long key = (v.G << kSlotBits) | (unsigned long long)j;
-    const bool sat = (key & h.ctrl) == h.cval;
-    const bool bit = (((key >> h.target) & 1ULL) != 0) != (h.flip != 0);
-    if (off) {
-        Cx<T> pa;
-        pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
-        pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
-        const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
-        if (is_swap(h.kind)) {
-            if (sat) {
-                v.amp = swap_update<T>(h.kind, bit, pa);
-                v.pres = pp;
-                v.dirty = true;
-            }
-        } else if (is_branch(h.kind)) {
-            const bool any = v.pres || pp;
-            if (__any_sync(kFull, sat && any)) {
-                const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
-                if (sat) {
-                    const bool keep = any && !negligible(o, pb);
-                    v.pres = keep;
-                    v.amp = keep ? o : czero<T>();
-                    v.dirty = true;
-                }
-            }
-        } else {
-            const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
-            if (__any_sync(kFull, need)) {
-                const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
-                if (need) { v.amp = o; v.dirty = true; }
-            }
-        }
-        return;
-    }
-    const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
-    if (__any_sync(kFull, need)) {
-        const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
-        if (need) { v.amp = o; v.dirty = true; }
-    }
-}
-
-// The cross-group gate of a pair pass, lane-local: a = slot of G0 (stored bit 0), b = slot of G1.
-template <class T>
-__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b, int j,
-                                          const PruneBits& pb) {
-    const unsigned long long key = (a.G << kSlotBits) | (unsigned long long)j;
-    const bool sat = (key & h.ctrl) == h.cval;
-    const bool bit_a = h.flip != 0, bit_b = !bit_a;
-    if (is_swap(h.kind)) {
-        if (sat) {
-            const Cx<T> na = swap_update<T>(h.kind, bit_a, b.amp), nb = swap_update<T>(h.kind, bit_b, a.amp);
-            const bool pa = b.pres, pbr = a.pres;
-            a.amp = na; b.amp = nb;
-            a.pres = pa; b.pres = pbr;
-            a.dirty = b.dirty = true;
-        }
-        return;
-    }
-    const bool any = a.pres || b.pres;
-    if (__any_sync(kFull, sat && any)) {
-        const Cx<T> oa = branch_update<T>(h.kind, g, bit_a, a.amp, b.amp);
-        const Cx<T> ob = branch_update<T>(h.kind, g, bit_b, b.amp, a.amp);
-        if (sat) {
-            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
-            a.pres = ka; a.amp = ka ? oa : czero<T>();
-            b.pres = kb; b.amp = kb ? ob : czero<T>();
-            a.dirty = b.dirty = true;
-        }
-    }
-}
-
-// Apply gates [g0, g1) to the two held slots; in a pair pass the first gate pairs them.
-// Lane 0 accumulates the amp-update count: every gate is credited with the present slots
-// it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
-template <class T>
-__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1,
-                                          bool pair_first, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
-                                          unsigned long long& upd) {
-    const int j = lane & 15;
-    for (uint32_t gi = g0; gi < g1; ++gi) {
-        const GateDesc* g = gates + gi;
-        const GateHead h = gate_head(g);
-        const unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
-        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
-        if (gi == g0 && pair_first) {
-            pair_step<T>(g, h, a, b, j, pb);
-            continue;
-        }
-        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : 0;
-        gate_step<T>(g, h, off, a, j, pb);
-        gate_step<T>(g, h, off, b, j, pb);
-    }
-}
-
-// Write a held slot back in place. A group absent at the start of the pass gets a bucket
-// (claimed by lane 0 of the half) when it ends up with a present key; every slot of a new
-// bucket is written. Returns the new bucket index on lane 0 of the half, else -1.
-template <class T>
-__device__ __forceinline__ long long write_val(const TableDev& t, unsigned ep, Val<T>& v, int lane,
-                                               unsigned int* status, unsigned long long& cnt_nnz,
-                                               unsigned long long& cnt_empty) {
-    const int j = lane & 15, half = lane >> 4;
-    const unsigned bal = __ballot_sync(kFull, v.pres);
-    const unsigned hm = half ? (bal >> 16) : (bal & 0xFFFFu);
-    long long b = v.b;
-    bool created = false;
-    long long fresh = -1;
-    if (__any_sync(kFull, b < 0 && hm != 0)) {
-        long long cb = -1;
-        if (b < 0 && hm && j == 0) cb = claim_group(t, ep, v.G, status, &created);
-        cb = (long long)shfl64((unsigned long long)cb, half << 4);
-        created = __shfl_sync(kFull, (int)created, half << 4) != 0;
-        if (b < 0 && hm) {
-            b = cb;
-            if (created && j == 0) fresh = b;
-        }
-    }
-    if (b >= 0) {
-        const size_t s = (size_t)b * kSlots + j;
-        if (created || v.pres != v.pres0)
-            t.keys[s] = v.pres ? ((v.G << kSlotBits) | (unsigned long long)j) : empty_key(j);
-        if (v.pres && v.dirty) store_amp<T>(t.amps, s, v.amp);
-        cnt_nnz += v.pres ? 1 : 0;
-        if (j == 0 && !hm) cnt_empty += 1;
-    }
-    return fresh;
-}
-
-// Append up to four new buckets (one candidate per half per held slot) to the live list.
-__device__ __forceinline__ void append_new(const TableDev& t, Ctl* ctl, long long fa, long long fb, int lane) {
-    const unsigned ma = __ballot_sync(kFull, fa >= 0), mb = __ballot_sync(kFull, fb >= 0);
-    const unsigned n = __popc(ma) + __popc(mb);
-    if (!n) return;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&ctl->list_tail, (unsigned long long)n);
-    base = shfl64(base, 0);
-    const unsigned below = (1u << lane) - 1u;
-    if (fa >= 0) t.list[base + __popc(ma & below)] = (unsigned)fa;
-    if (fb >= 0) t.list[base + __popc(ma) + __popc(mb & below)] = (unsigned)fb;
-}
-
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
     for (int o = 16; o; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;
@@ -245,119 +42,6 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;
-}
-
-// Block-reduce the pass counters; the last block to finish publishes the pass (key count,
-// list length, empty buckets, pass counter, amp updates, algorithmic bytes). Nothing is
-// published when a pass failed.
-__device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e, unsigned long long u,
-                            unsigned long long nnz_in, bool keys_fixed, unsigned amp_bytes) {
-    __shared__ unsigned long long red[3][kThreads / 32];
-    __shared__ bool last;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    n = warp_sum(n); e = warp_sum(e); u = warp_sum(u);
-    if (lane == 0) { red[0][w] = n; red[1][w] = e; red[2][w] = u; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long bn = 0, be = 0, bu = 0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { bn += red[0][i]; be += red[1][i]; bu += red[2][i]; }
-        if (bn) atomicAdd(&ctl->acc_nnz, bn);
-        if (be) atomicAdd(&ctl->acc_empty, be);
-        if (bu) atomicAdd(&ctl->acc_upd, bu);
-        __threadfence();
-        const unsigned prev = atomicAdd(&ctl->done, 1u);
-        last = prev == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        const unsigned long long tn = atomicExch(&ctl->acc_nnz, 0ULL);
-        const unsigned long long te = atomicExch(&ctl->acc_empty, 0ULL);
-        const unsigned long long tu = atomicExch(&ctl->acc_upd, 0ULL);
-        if (*(volatile unsigned int*)&ctl->status == 0) {
-            ctl->nnz = tn;
-            ctl->empty_groups = te;
-            ctl->list_n = *(volatile unsigned long long*)&ctl->list_tail;
-            ctl->amp_updates += tu;
-            ctl->alg_bytes += keys_fixed ? nnz_in * (8ULL + 2ULL * amp_bytes) : (nnz_in + tn) * (8ULL + amp_bytes);
-            ctl->seq += 1;
-        }
-        ctl->done = 0;
-        __threadfence();
-    }
-}
-
-template <class T, bool PAIR>
-__global__ void __launch_bounds__(kThreads, 3) pass_kernel(PassArgs a) {
-    Ctl* ctl = a.ctl;
-    if (*(volatile unsigned int*)&ctl->status) return;
-    const unsigned long long n = ctl->list_n;
-    if (PAIR && 2 * n > a.max_groups) {   // could overflow: refuse before touching the state
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
-        return;
-    }
-    const unsigned ep = ctl->epoch;
-    const unsigned long long nnz_in = ctl->nnz;
-    const TableDev t = a.t;
-    const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
-    Val<T> va, vb;
-
-    if (!PAIR) {
-        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
-            const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
-            const long long ba = ea < n ? (long long)t.list[ea] : -1;
-            const long long bb = eb < n ? (long long)t.list[eb] : -1;
-            const unsigned long long Ga = ba >= 0 ? load_hdr(t.hdr + ba).group : 0ULL;
-            const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
-            load_val<T>(t, va, Ga, ba, j);
-            load_val<T>(t, vb, Gb, bb, j);
-            run_gates<T>(a.gates, a.g0, a.g1, false, va, vb, lane, a.prune, upd);
-            write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
-            write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
-        }
-    } else {
-        const uint32_t q = __ldg(&a.gates[a.g0].target);
-        const unsigned long long m = 1ULL << (q - kSlotBits);
-        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
-            // lanes 0..3: one list entry each -> ownership and the pair's buckets
-            bool owner = false;
-            long long b0 = -1, b1 = -1;
-            unsigned long long G0 = 0;
-            if (lane < 4 && e0 + lane < n) {
-                const long long b = (long long)t.list[e0 + lane];
-                const unsigned long long G = load_hdr(t.hdr + b).group;
-                const bool mine1 = (G & m) != 0;
-                const long long bp = lookup_group(t, ep, G ^ m);
-                owner = !mine1 || bp < 0;
-                b0 = mine1 ? bp : b;
-                b1 = mine1 ? b : bp;
-                G0 = G & ~m;
-            }
-            unsigned om = __ballot_sync(kFull, owner) & 0xFu;
-            while (om) {
-                const int u0 = __ffs(om) - 1;
-                om &= om - 1;
-                int u1 = -1;
-                if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
-                const int u = half ? u1 : u0;
-                const int src = u >= 0 ? u : u0;
-                const long long ub0 = (long long)shfl64((unsigned long long)b0, src);
-                const long long ub1 = (long long)shfl64((unsigned long long)b1, src);
-                const unsigned long long uG0 = shfl64(G0, src);
-                const bool act = u >= 0;
-                load_val<T>(t, va, uG0, act ? ub0 : -1, j);
-                load_val<T>(t, vb, uG0 | m, act ? ub1 : -1, j);
-                run_gates<T>(a.gates, a.g0, a.g1, true, va, vb, lane, a.prune, upd);
-                const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
-                const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
-                append_new(t, ctl, fa, fb, lane);
-            }
-        }
-    }
-    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, a.amp_bytes);
 }
 
 // |0...0>: new epoch (every bucket becomes free), claim group 0, store key 0 with amplitude 1.
@@ -670,38 +354,6 @@ int grid_for(unsigned long long work_items, int per_block, int sms) {
 }
 
 }  // namespace
-
-// Resident blocks per SM of each pass-kernel instantiation (queried once per process).
-int pass_residency(bool dbl, bool pair) {
-    static int cache[4] = {0, 0, 0, 0};
-    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
-    if (!c) {
-        int n = 0;
-        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<double, true>, kThreads, 0);
-        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<double, false>, kThreads, 0);
-        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<float, true>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pass_kernel<float, false>, kThreads, 0);
-        c = n > 0 ? n : 1;
-    }
-    return c;
-}
-
-cudaError_t launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
-    // list_hint bounds the live-bucket count; the grid is sized from it (a warp takes four
-    // list entries per step) and capped at one resident wave; the kernel reads the exact
-    // count on the device.
-    unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
-    const unsigned long long wave = (unsigned long long)sms * pass_residency(dbl, a.pair != 0);
-    const int grid = (int)std::max<unsigned long long>(1, std::min(g, wave));
-    if (dbl) {
-        if (a.pair) pass_kernel<double, true><<<grid, kThreads, 0, st>>>(a);
-        else pass_kernel<double, false><<<grid, kThreads, 0, st>>>(a);
-    } else {
-        if (a.pair) pass_kernel<float, true><<<grid, kThreads, 0, st>>>(a);
-        else pass_kernel<float, false><<<grid, kThreads, 0, st>>>(a);
-    }
-    return cudaGetLastError();
-}
 
 cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st) {
     set_zero_kernel<<<1, 32, 0, st>>>(t, ctl, dbl ? 1 : 0);

@@ -1,0 +1,662 @@
+// Gate-pass kernels of the sparse statevector engine (sm_103a).
+//
+// A gate pass updates the table in place; it walks the list of live buckets.
+//  * stream pass: a run of gates that never pair keys across 16-key groups -- diagonal gates
+//    on any qubit and any gate on qubits 0..3 (the partner sits in the same bucket and is
+//    reached with a warp shuffle). A consumer half-warp holds two buckets (lane j holds slot
+//    j of both).
+//  * pair pass: a gate whose partner key lives in another group (branching gate on a qubit
+//    >= 4, or X/Y on a qubit >= 4 with controls the host could not resolve), followed by a
+//    stream run. A consumer half-warp takes the group pair (G0, G1 = G0 | m): lane j holds
+//    slot j of both groups, so the pair update is lane-local. The group with stored target
+//    bit 0 owns the pair; the other owns it only when its partner group is absent -- the
+//    reference's pair rule (emulator/device/device_table_FC.cuh:62-110) lifted from keys to
+//    16-key groups, which gives the same pairs and the same per-key results. A resolve
+//    kernel settles ownership for every list entry before the pass.
+// Data movement: every warp prefetches the buckets of its next slots into its own ring of
+// shared-memory slots with cp.async (16-byte copies, one commit group per slot), so several
+// slots are in flight while it computes; it moves the current slot into registers, applies
+// the gates and writes the results back in place with ordinary stores. Every
+// pair with at least one present member is read once and written once. A group that appears
+// for the first time is claimed with a 128-bit CAS and appended to the list (such groups are
+// beyond the pass's range). Pruning follows the reference
+// (emulator/device/device_data.cuh:108-156): branching gates drop negligible outputs, swap
+// and diagonal gates keep every key.
+#include "sqc_kernels.h"
+
+#include <algorithm>
+
+namespace sqc {
+
+namespace {
+
+template <class T> struct AmpT;
+template <> struct AmpT<double> { using V = double2; };
+template <> struct AmpT<float> { using V = float2; };
+
+template <class T> __device__ __forceinline__ Cx<T> czero() { return Cx<T>{T(0), T(0)}; }
+
+__device__ __forceinline__ unsigned long long umin64(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
+
+template <class T>
+__device__ __forceinline__ void store_amp(void* amps, size_t s, Cx<T> a) {
+    typename AmpT<T>::V v;
+    v.x = a.r;
+    v.y = a.i;
+    reinterpret_cast<typename AmpT<T>::V*>(amps)[s] = v;
+}
+
+__device__ __forceinline__ bool slot_present(unsigned long long key, int j) { return (int)(key & 15ULL) == j; }
+
+// One slot held by a lane: its group, amplitude and presence, where it lives (b = -1 for a
+// group absent at the start of the pass) and whether the pass changed it.
+template <class T> struct Val {
+    unsigned long long G;
+    long long b;
+    Cx<T> amp;
+    bool pres, pres0, dirty;
+};
+
+struct GateHead {
+    uint32_t kind, target, flip, credit;
+    unsigned long long ctrl, cval;
+};
+
+__device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
+    GateHead h;
+    h.kind = __ldg(&g->kind);
+    h.target = __ldg(&g->target);
+    h.flip = __ldg(&g->flip);
+    h.credit = __ldg(&g->pad);
+    h.ctrl = __ldg(&g->ctrl);
+    h.cval = __ldg(&g->cval);
+    return h;
+}
+
+// One streamable gate on one held slot. `off` is the lane distance to the partner slot
+// (1 << q for q < 4, inside the half-warp) or 0 for a diagonal gate on a qubit >= 4.
+template <class T>
+__device__ __forceinline__ void gate_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
+                                          const PruneBits& pb) {
+    const unsigned long long key = (v.G << kSlotBits) | (unsigned long long)j;
+    const bool sat = (key & h.ctrl) == h.cval;
+    const bool bit = (((key >> h.target) & 1ULL) != 0) != (h.flip != 0);
+    if (off) {
+        Cx<T> pa;
+        pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
+        pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
+        const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
+        if (is_swap(h.kind)) {
+            if (sat) {
+                v.amp = swap_update<T>(h.kind, bit, pa);
+                v.pres = pp;
+                v.dirty = true;
+            }
+        } else if (is_branch(h.kind)) {
+            const bool any = v.pres || pp;
+            if (__any_sync(kFull, sat && any)) {
+                const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
+                if (sat) {
+                    const bool keep = any && !negligible(o, pb);
+                    v.pres = keep;
+                    v.amp = keep ? o : czero<T>();
+                    v.dirty = true;
+                }
+            }
+        } else {
+            const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
+            if (__any_sync(kFull, need)) {
+                const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
+                if (need) { v.amp = o; v.dirty = true; }
+            }
+        }
+        return;
+    }
+    const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
+    if (__any_sync(kFull, need)) {
+        const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
+        if (need) { v.amp = o; v.dirty = true; }
+    }
+}
+
+// The cross-group gate of a pair pass, lane-local: a = slot of G0 (stored bit 0), b = slot of G1.
+template <class T>
+__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b, int j,
+                                          const PruneBits& pb) {
+    const unsigned long long key = (a.G << kSlotBits) | (unsigned long long)j;
+    const bool sat = (key & h.ctrl) == h.cval;
+    const bool bit_a = h.flip != 0, bit_b = !bit_a;
+    if (is_swap(h.kind)) {
+        if (sat) {
+            const Cx<T> na = swap_update<T>(h.kind, bit_a, b.amp), nb = swap_update<T>(h.kind, bit_b, a.amp);
+            const bool pa = b.pres, pbr = a.pres;
+            a.amp = na; b.amp = nb;
+            a.pres = pa; b.pres = pbr;
+            a.dirty = b.dirty = true;
+        }
+        return;
+    }
+    const bool any = a.pres || b.pres;
+    if (__any_sync(kFull, sat && any)) {
+        const Cx<T> oa = branch_update<T>(h.kind, g, bit_a, a.amp, b.amp);
+        const Cx<T> ob = branch_update<T>(h.kind, g, bit_b, b.amp, a.amp);
+        if (sat) {
+            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+            a.pres = ka; a.amp = ka ? oa : czero<T>();
+            b.pres = kb; b.amp = kb ? ob : czero<T>();
+            a.dirty = b.dirty = true;
+        }
+    }
+}
+
+// Apply gates [g0, g1) to the two held slots; in a pair pass the first gate pairs them.
+// Lane 0 accumulates the amp-update count: every gate is credited with the present slots
+// it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
+template <class T>
+__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1,
+                                          bool pair_first, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
+                                          unsigned long long& upd) {
+    const int j = lane & 15;
+    for (uint32_t gi = g0; gi < g1; ++gi) {
+        const GateDesc* g = gates + gi;
+        const GateHead h = gate_head(g);
+        const unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        if (gi == g0 && pair_first) {
+            pair_step<T>(g, h, a, b, j, pb);
+            continue;
+        }
+        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : 0;
+        gate_step<T>(g, h, off, a, j, pb);
+        gate_step<T>(g, h, off, b, j, pb);
+    }
+}
+
+// Write a held slot back in place. A group absent at the start of the pass gets a bucket
+// (claimed by lane 0 of the half) when it ends up with a present key; every slot of a new
+// bucket is written. Returns the new bucket index on lane 0 of the half, else -1.
+template <class T>
+__device__ __forceinline__ long long write_val(const TableDev& t, unsigned ep, Val<T>& v, int lane,
+                                               unsigned int* status, unsigned long long& cnt_nnz,
+                                               unsigned long long& cnt_empty) {
+    const int j = lane & 15, half = lane >> 4;
+    const unsigned bal = __ballot_sync(kFull, v.pres);
+    const unsigned hm = half ? (bal >> 16) : (bal & 0xFFFFu);
+    long long b = v.b;
+    bool created = false;
+    long long fresh = -1;
+    if (__any_sync(kFull, b < 0 && hm != 0)) {
+        long long cb = -1;
+        if (b < 0 && hm && j == 0) cb = claim_group(t, ep, v.G, status, &created);
+        cb = (long long)shfl64((unsigned long long)cb, half << 4);
+        created = __shfl_sync(kFull, (int)created, half << 4) != 0;
+        if (b < 0 && hm) {
+            b = cb;
+            if (created && j == 0) fresh = b;
+        }
+    }
+    if (b >= 0) {
+        const size_t s = (size_t)b * kSlots + j;
+        if (created || v.pres != v.pres0)
+            t.keys[s] = v.pres ? ((v.G << kSlotBits) | (unsigned long long)j) : empty_key(j);
+        if (v.pres && v.dirty) store_amp<T>(t.amps, s, v.amp);
+        cnt_nnz += v.pres ? 1 : 0;
+        if (j == 0 && !hm) cnt_empty += 1;
+    }
+    return fresh;
+}
+
+// Append up to four new buckets (one candidate per half per held slot) to the live list.
+__device__ __forceinline__ void append_new(const TableDev& t, Ctl* ctl, long long fa, long long fb, int lane) {
+    const unsigned ma = __ballot_sync(kFull, fa >= 0), mb = __ballot_sync(kFull, fb >= 0);
+    const unsigned n = __popc(ma) + __popc(mb);
+    if (!n) return;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->list_tail, (unsigned long long)n);
+    base = shfl64(base, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (fa >= 0) t.list[base + __popc(ma & below)] = (unsigned)fa;
+    if (fb >= 0) t.list[base + __popc(ma) + __popc(mb & below)] = (unsigned)fb;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
+
+// Block-reduce the pass counters; the last block to finish publishes the pass (key count,
+// list length, empty buckets, pass counter, amp updates, algorithmic bytes). Nothing is
+// published when a pass failed.
+__device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e, unsigned long long u,
+                            unsigned long long nnz_in, bool keys_fixed, unsigned amp_bytes) {
+    __shared__ unsigned long long red[3][32];
+    __shared__ bool last;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    n = warp_sum(n); e = warp_sum(e); u = warp_sum(u);
+    if (lane == 0) { red[0][w] = n; red[1][w] = e; red[2][w] = u; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bn = 0, be = 0, bu = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { bn += red[0][i]; be += red[1][i]; bu += red[2][i]; }
+        if (bn) atomicAdd(&ctl->acc_nnz, bn);
+        if (be) atomicAdd(&ctl->acc_empty, be);
+        if (bu) atomicAdd(&ctl->acc_upd, bu);
+        __threadfence();
+        const unsigned prev = atomicAdd(&ctl->done, 1u);
+        last = prev == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long tn = atomicExch(&ctl->acc_nnz, 0ULL);
+        const unsigned long long te = atomicExch(&ctl->acc_empty, 0ULL);
+        const unsigned long long tu = atomicExch(&ctl->acc_upd, 0ULL);
+        if (*(volatile unsigned int*)&ctl->status == 0) {
+            ctl->nnz = tn;
+            ctl->empty_groups = te;
+            ctl->list_n = *(volatile unsigned long long*)&ctl->list_tail;
+            ctl->amp_updates += tu;
+            ctl->alg_bytes += keys_fixed ? nnz_in * (8ULL + 2ULL * amp_bytes) : (nnz_in + tn) * (8ULL + amp_bytes);
+            ctl->seq += 1;
+        }
+        ctl->done = 0;
+        __threadfence();
+    }
+}
+
+// ---- direct pass (tables up to kDirectMaxBuckets) ------------------------------------------
+// For small states the extra launch and the pipeline fill of a staged pass cost more than
+// they save: each warp takes four list entries at a time, settles ownership inline (four
+// lookups in parallel), packs owned pairs two per warp and loads its slots straight into
+// registers.
+template <class T>
+__device__ __forceinline__ void load_val_g(const TableDev& t, Val<T>& v, unsigned long long G, long long b, int j) {
+    v.G = G;
+    v.b = b;
+    v.dirty = false;
+    v.pres = false;
+    v.amp = czero<T>();
+    if (b >= 0) {
+        const size_t s = (size_t)b * kSlots + j;
+        v.pres = slot_present(t.keys[s], j);
+        if (v.pres) {
+            const typename AmpT<T>::V x = reinterpret_cast<const typename AmpT<T>::V*>(t.amps)[s];
+            v.amp = Cx<T>{x.x, x.y};
+        }
+    }
+    v.pres0 = v.pres;
+}
+
+template <class T, bool PAIR>
+__global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
+    Ctl* ctl = a.ctl;
+    if (*(volatile unsigned int*)&ctl->status) return;
+    const unsigned long long n = ctl->list_n;
+    if (PAIR && 2 * n > a.max_groups) {   // could overflow: refuse before touching the state
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
+        return;
+    }
+    const unsigned ep = ctl->epoch;
+    const unsigned long long nnz_in = ctl->nnz;
+    const TableDev t = a.t;
+    const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
+    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
+    Val<T> va, vb;
+    if (!PAIR) {
+        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+            const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
+            const long long ba = ea < n ? (long long)t.list[ea] : -1;
+            const long long bb = eb < n ? (long long)t.list[eb] : -1;
+            const unsigned long long Ga = ba >= 0 ? load_hdr(t.hdr + ba).group : 0ULL;
+            const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
+            load_val_g<T>(t, va, Ga, ba, j);
+            load_val_g<T>(t, vb, Gb, bb, j);
+            run_gates<T>(a.gates, a.g0, a.g1, false, va, vb, lane, a.prune, upd);
+            write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+            write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        }
+    } else {
+        const uint32_t q = __ldg(&a.gates[a.g0].target);
+        const unsigned long long m = 1ULL << (q - kSlotBits);
+        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+            // lanes 0..3: one list entry each -> ownership and the pair's buckets
+            bool owner = false;
+            long long b0 = -1, b1 = -1;
+            unsigned long long G0 = 0;
+            if (lane < 4 && e0 + lane < n) {
+                const long long b = (long long)t.list[e0 + lane];
+                const unsigned long long G = load_hdr(t.hdr + b).group;
+                const bool mine1 = (G & m) != 0;
+                const long long bp = lookup_group(t, ep, G ^ m);
+                owner = !mine1 || bp < 0;
+                b0 = mine1 ? bp : b;
+                b1 = mine1 ? b : bp;
+                G0 = G & ~m;
+            }
+            unsigned om = __ballot_sync(kFull, owner) & 0xFu;
+            while (om) {
+                const int u0 = __ffs(om) - 1;
+                om &= om - 1;
+                int u1 = -1;
+                if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
+                const int u = half ? u1 : u0;
+                const int src = u >= 0 ? u : u0;
+                const long long ub0 = (long long)shfl64((unsigned long long)b0, src);
+                const long long ub1 = (long long)shfl64((unsigned long long)b1, src);
+                const unsigned long long uG0 = shfl64(G0, src);
+                const bool act = u >= 0;
+                load_val_g<T>(t, va, uG0, act ? ub0 : -1, j);
+                load_val_g<T>(t, vb, uG0 | m, act ? ub1 : -1, j);
+                run_gates<T>(a.gates, a.g0, a.g1, true, va, vb, lane, a.prune, upd);
+                const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+                const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+                append_new(t, ctl, fa, fb, lane);
+            }
+        }
+    }
+    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, a.amp_bytes);
+}
+
+// ---- resolve: ownership of every group pair, before a pair pass ---------------------------
+// The list is cut into ranges of R entries (R a multiple of 32, a power of two). One warp per
+// range writes the range's owned pairs densely at units[r*R ...] (warp ballot, no atomics)
+// and their number to counts[r].
+__global__ void __launch_bounds__(256) resolve_kernel(PassArgs a) {
+    Ctl* ctl = a.ctl;
+    if (*(volatile unsigned int*)&ctl->status) return;
+    const unsigned long long n = ctl->list_n;
+    if (2 * n > a.max_groups) {   // the pass could overflow the table: refuse before touching the state
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
+        return;
+    }
+    const unsigned ep = ctl->epoch;
+    const uint32_t q = __ldg(&a.gates[a.g0].target);
+    const unsigned long long m = 1ULL << (q - kSlotBits);
+    const TableDev t = a.t;
+    const unsigned long long R = a.range;
+    const unsigned long long nranges = (n + R - 1) / R;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long r = gw; r < nranges; r += nw) {
+        const unsigned long long e0 = r * R, e1 = umin64(n, e0 + R);
+        unsigned cnt = 0;
+        for (unsigned long long e = e0 + lane; e - lane < e1; e += 32) {
+            Unit u;
+            bool own = false;
+            if (e < e1) {
+                const unsigned b = t.list[e];
+                const unsigned long long G = load_hdr(t.hdr + b).group;
+                const bool mine1 = (G & m) != 0;
+                const long long bp = lookup_group(t, ep, G ^ m);
+                own = !mine1 || bp < 0;
+                u.G0 = G & ~m;
+                u.b0 = mine1 ? kNoBucket : b;
+                u.b1 = mine1 ? b : (bp < 0 ? kNoBucket : (unsigned)bp);
+            }
+            const unsigned om = __ballot_sync(kFull, own);
+            if (own) t.units[e0 + cnt + __popc(om & ((1u << lane) - 1u))] = u;
+            cnt += __popc(om);
+        }
+        if (lane == 0) t.counts[r] = cnt;
+    }
+}
+
+// ---- staged pass -------------------------------------------------------------------------
+// Every warp is a worker with its own ring of kDepth shared-memory slots. It copies the
+// buckets of the slot kDepth-1 steps ahead with cp.async (one commit group per slot), waits
+// for the current slot's group, moves the slot into registers, applies the gates and writes
+// back in place. A slot holds four buckets: four list entries (stream pass) or two owned
+// pairs (pair pass).
+constexpr int kWarpsPerBlock = 4;
+constexpr int kStagedThreads = 32 * kWarpsPerBlock;
+constexpr int kDepth = 4;
+
+template <class T> struct Slot {
+    unsigned long long keys[4][kSlots];
+    typename AmpT<T>::V amps[4][kSlots];
+    Header hdr[4];              // stream passes: copied headers (groups)
+    unsigned long long G[4];    // pair passes: group of each held bucket
+    unsigned int b[4];          // bucket index, kNoBucket when absent
+    int n;                      // 0: nothing more for this warp
+    int pad[3];
+};
+
+template <class T>
+__device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsigned b, const Slot<T>& sl, int k,
+                                           int j) {
+    v.G = G;
+    v.b = b == kNoBucket ? -1 : (long long)b;
+    v.dirty = false;
+    v.pres = false;
+    v.amp = czero<T>();
+    if (b != kNoBucket) {
+        v.pres = slot_present(sl.keys[k][j], j);
+        if (v.pres) {
+            const typename AmpT<T>::V x = sl.amps[k][j];
+            v.amp = Cx<T>{x.x, x.y};
+        }
+    }
+    v.pres0 = v.pres;
+}
+
+// Where a warp's next slot comes from: a strided sequence of 4-entry items (stream pass) or
+// the dense owned pairs of a strided sequence of ranges (pair pass).
+struct SlotSource {
+    unsigned long long next;      // stream: next item; pair: current range
+    unsigned long long u, c;      // pair: next unit within the range, units in the range
+    unsigned long long stride, end;
+};
+
+template <class T, bool PAIR>
+__device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotSource& src, unsigned long long n,
+                                           unsigned long long R, unsigned long long m, int lane) {
+    constexpr uint32_t kAmp = (uint32_t)(sizeof(typename AmpT<T>::V) * kSlots);
+    constexpr int kKeyChunks = 128 / 16, kAmpChunks = (int)(kAmp / 16);
+    constexpr int kChunks = 4 * (kKeyChunks + kAmpChunks) + (PAIR ? 0 : 4);
+    unsigned bk = kNoBucket;
+    unsigned long long Gk = 0;
+    bool any = false;
+    if (!PAIR) {
+        if (src.next < src.end) {
+            const unsigned long long e = 4 * src.next + (unsigned long long)lane;
+            if (lane < 4 && e < n) bk = t.list[e];
+            src.next += src.stride;
+            any = true;
+        }
+    } else {
+        while (src.next < src.end && src.u >= src.c) {   // move to the next range with pairs
+            src.next += src.stride;
+            src.u = 0;
+            src.c = src.next < src.end ? t.counts[src.next] : 0;
+        }
+        if (src.next < src.end) {
+            const unsigned long long base = src.next * R + src.u;
+            const bool second = src.u + 1 < src.c;
+            const int k = lane & 3;
+            if (lane < 4 && (k < 2 || second)) {
+                const Unit un = t.units[base + (k >> 1)];
+                bk = (k & 1) ? un.b1 : un.b0;
+                Gk = (k & 1) ? (un.G0 | m) : un.G0;
+            }
+            src.u += 2;
+            any = true;
+        }
+    }
+    const unsigned b0 = __shfl_sync(kFull, bk, 0), b1 = __shfl_sync(kFull, bk, 1);
+    const unsigned b2 = __shfl_sync(kFull, bk, 2), b3 = __shfl_sync(kFull, bk, 3);
+    if (lane < 4) {
+        sl.b[lane] = bk;
+        sl.G[lane] = Gk;
+    }
+    if (lane == 0) sl.n = any ? 1 : 0;
+    for (int c = lane; c < kChunks; c += 32) {
+        int k, off;
+        const char* s;
+        char* d;
+        if (c < 4 * kKeyChunks) {
+            k = c / kKeyChunks; off = (c % kKeyChunks) * 16;
+        } else if (c < 4 * (kKeyChunks + kAmpChunks)) {
+            const int x = c - 4 * kKeyChunks;
+            k = x / kAmpChunks; off = (x % kAmpChunks) * 16;
+        } else {
+            k = c - 4 * (kKeyChunks + kAmpChunks); off = 0;
+        }
+        const unsigned b = k == 0 ? b0 : k == 1 ? b1 : k == 2 ? b2 : b3;
+        if (b == kNoBucket) continue;
+        if (c < 4 * kKeyChunks) {
+            s = reinterpret_cast<const char*>(t.keys + (size_t)b * kSlots) + off;
+            d = reinterpret_cast<char*>(sl.keys[k]) + off;
+        } else if (c < 4 * (kKeyChunks + kAmpChunks)) {
+            s = reinterpret_cast<const char*>(t.amps) + (size_t)b * kAmp + off;
+            d = reinterpret_cast<char*>(sl.amps[k]) + off;
+        } else {
+            s = reinterpret_cast<const char*>(t.hdr + b);
+            d = reinterpret_cast<char*>(&sl.hdr[k]);
+        }
+        cp_async16(d, s);
+    }
+    cp_async_commit();
+}
+
+template <class T, bool PAIR>
+__global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Slot<T>* ring = reinterpret_cast<Slot<T>*>(smem_raw) + (threadIdx.x >> 5) * kDepth;
+
+    Ctl* ctl = a.ctl;
+    if (*(volatile unsigned int*)&ctl->status) return;
+    const unsigned long long n = ctl->list_n;
+    const unsigned ep = ctl->epoch;
+    const unsigned long long nnz_in = ctl->nnz;
+    const TableDev t = a.t;
+    const int lane = threadIdx.x & 31, half = lane >> 4, jj = lane & 15;
+    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    const unsigned long long R = a.range;
+    const unsigned long long m = PAIR ? 1ULL << (__ldg(&a.gates[a.g0].target) - kSlotBits) : 0ULL;
+    SlotSource src;
+    src.next = gw;
+    src.stride = nw;
+    src.u = 0;
+    if (!PAIR) {
+        src.end = (n + 3) / 4;
+        src.c = 0;
+    } else {
+        src.end = (n + R - 1) / R;
+        src.c = src.next < src.end ? t.counts[src.next] : 0;
+    }
+    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
+    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, PAIR>(ring[d], t, src, n, R, m, lane);
+    Val<T> va, vb;
+    for (unsigned long long step = 0;; ++step) {
+        issue_slot<T, PAIR>(ring[(step + kDepth - 1) % kDepth], t, src, n, R, m, lane);
+        cp_async_wait<kDepth - 1>();
+        __syncwarp();
+        const Slot<T>& sl = ring[step % kDepth];
+        if (sl.n == 0) break;
+        const int ka = 2 * half, kb = ka + 1;
+        const unsigned ba = sl.b[ka], bb = sl.b[kb];
+        unsigned long long Ga, Gb;
+        if (PAIR) {
+            Ga = sl.G[ka];
+            Gb = sl.G[kb];
+        } else {
+            Ga = ba != kNoBucket ? sl.hdr[ka].group : 0ULL;
+            Gb = bb != kNoBucket ? sl.hdr[kb].group : 0ULL;
+        }
+        load_val_s<T>(va, Ga, ba, sl, ka, jj);
+        load_val_s<T>(vb, Gb, bb, sl, kb, jj);
+        __syncwarp();
+        run_gates<T>(a.gates, a.g0, a.g1, PAIR, va, vb, lane, a.prune, upd);
+        const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+        const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        if (PAIR) append_new(t, ctl, fa, fb, lane);
+    }
+    cp_async_wait<0>();   // nothing may still be landing in shared memory when the block exits
+    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, a.amp_bytes);
+}
+
+template <class T>
+constexpr size_t staged_smem() {
+    return (size_t)kWarpsPerBlock * kDepth * sizeof(Slot<T>);
+}
+
+// Resident blocks per SM of each staged-kernel instantiation (queried once per process).
+int staged_residency(bool dbl, bool pair) {
+    static int cache[4] = {0, 0, 0, 0};
+    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
+    if (!c) {
+        int n = 0;
+        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<double, true>, kStagedThreads, staged_smem<double>());
+        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<double, false>, kStagedThreads, staged_smem<double>());
+        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<float, true>, kStagedThreads, staged_smem<float>());
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<float, false>, kStagedThreads, staged_smem<float>());
+        c = n > 0 ? n : 1;
+    }
+    return c;
+}
+
+int direct_residency(bool dbl, bool pair) {
+    static int cache[4] = {0, 0, 0, 0};
+    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
+    if (!c) {
+        int n = 0;
+        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<double, true>, kThreads, 0);
+        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<double, false>, kThreads, 0);
+        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<float, true>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<float, false>, kThreads, 0);
+        c = n > 0 ? n : 1;
+    }
+    return c;
+}
+
+constexpr unsigned long long kDirectMaxBuckets = 1ULL << 20;
+
+}  // namespace
+
+// One warp ballot per range: the finest split, which spreads small states over every warp
+// and gives large ones many ranges per warp.
+unsigned long long pass_range(unsigned long long, int) { return 32; }
+
+int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
+    // list_hint bounds the live-bucket count; grids are sized from it (one resident wave at
+    // most); the kernels read the exact count. Tables of up to kDirectMaxBuckets buckets
+    // (states that have never needed more) take the direct pass.
+    if (a.t.mask + 1 <= kDirectMaxBuckets) {
+        const unsigned long long wave = (unsigned long long)sms * direct_residency(dbl, a.pair != 0);
+        const unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
+        const int grid = (int)std::max<unsigned long long>(1, std::min(g, wave));
+        if (dbl) {
+            if (a.pair) direct_kernel<double, true><<<grid, kThreads, 0, st>>>(a);
+            else direct_kernel<double, false><<<grid, kThreads, 0, st>>>(a);
+        } else {
+            if (a.pair) direct_kernel<float, true><<<grid, kThreads, 0, st>>>(a);
+            else direct_kernel<float, false><<<grid, kThreads, 0, st>>>(a);
+        }
+        return cudaGetLastError() == cudaSuccess ? 1 : -1;
+    }
+    int launched = 0;
+    if (a.pair) {
+        const unsigned long long nranges = list_hint / a.range + 1;
+        const unsigned long long rg = std::min<unsigned long long>((nranges + 7) / 8, (unsigned long long)sms * 8);
+        resolve_kernel<<<(int)std::max<unsigned long long>(rg, 1), 256, 0, st>>>(a);
+        ++launched;
+    }
+    const unsigned long long items = a.pair ? list_hint / 2 + 1 : (list_hint + 3) / 4;
+    const unsigned long long wave = (unsigned long long)sms * staged_residency(dbl, a.pair != 0);
+    const int grid = (int)std::max<unsigned long long>(1, std::min(wave, (items + 3) / 4));
+    if (dbl) {
+        if (a.pair) staged_kernel<double, true><<<grid, kStagedThreads, staged_smem<double>(), st>>>(a);
+        else staged_kernel<double, false><<<grid, kStagedThreads, staged_smem<double>(), st>>>(a);
+    } else {
+        if (a.pair) staged_kernel<float, true><<<grid, kStagedThreads, staged_smem<float>(), st>>>(a);
+        else staged_kernel<float, false><<<grid, kStagedThreads, staged_smem<float>(), st>>>(a);
+    }
+    ++launched;
+    return cudaGetLastError() == cudaSuccess ? launched : -1;
+}
+
+}  // namespace sqc

@@ -15,7 +15,8 @@ enum Status : unsigned int {
     ST_OK = 0,
     ST_TABLE_FULL = 1,   // a claim found no free bucket within kMaxProbe (state no longer valid)
     ST_DUPLICATE = 2,    // set_state saw the same key twice
-    ST_GROW = 3          // a pair pass refused to start: the table might overflow (state intact)
+    ST_GROW = 3,         // a pair pass refused to start: the table might overflow (state intact)
+    ST_TIMEOUT = 4       // a bounded wait inside a pass ran out (state no longer valid)
 };
 
 // gate kinds (0..12 = sqc_gate.kind); KYPH is internal: the diagonal left over when an
@@ -28,11 +29,22 @@ struct alignas(16) Header {
     unsigned int aux;           // 0
 };
 
+// One group pair of a pair pass, resolved before the pass: G0 has the stored target bit 0;
+// b0/b1 are the buckets of G0 and G0 | m (kNoBucket when absent). Written per list entry;
+// entries whose group does not own its pair hold b0 = b1 = kNoBucket.
+constexpr unsigned kNoBucket = 0xFFFFFFFFu;
+struct alignas(16) Unit {
+    unsigned long long G0;
+    unsigned int b0, b1;
+};
+
 struct TableDev {
     Header* hdr;
     unsigned long long* keys;
     void* amps;
     unsigned int* list;         // live buckets, in claim order
+    Unit* units;                // owned pairs of a pair pass, dense per range of list entries
+    unsigned int* counts;       // owned pairs per range (nb / 32 entries)
     unsigned long long mask;    // nb - 1
 };
 
@@ -86,6 +98,7 @@ struct PassArgs {
     uint32_t credit;        // gates resolved on the host just before this pass (identity or
                             // relabel): each is credited with this pass's input key count
     unsigned long long max_groups;   // a pair pass refuses to start above max_groups / 2 buckets
+    unsigned long long range;        // list entries per resolve range (power of two, >= 32)
     PruneBits prune;
 };
 

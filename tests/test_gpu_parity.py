@@ -54,6 +54,33 @@ def test_random_circuits_bitexact(seed, precision):
     assert stats["amp_updates"] == upd
 
 
+STAGED_BUCKETS = 1 << 21   # tables above 2^20 buckets take the staged (cp.async pipelined) passes
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("precision", [64, 32])
+def test_random_circuits_bitexact_staged_path(seed, precision):
+    rng = circuits.SplitMix64(circuits.stream_seed("gpu-staged", seed))
+    nq = (12, 20, 30, 44, 64, 64)[seed]
+    k = min(nq, 8 + seed)
+    g = circuits.random_circuit(nq, k, 250, 3, rng, kinds=ALL_KINDS)
+    got, stats = run_gpu(nq, g, precision, initial_buckets=STAGED_BUCKETS)
+    want, upd = run_oracle(g, precision)
+    assert_identical(got, want)
+    assert stats["amp_updates"] == upd
+
+
+def test_growth_from_direct_into_staged_tables():
+    """A state that outgrows 2^20 buckets moves from direct to staged passes mid-circuit."""
+    rng = circuits.SplitMix64(circuits.stream_seed("grow-staged"))
+    g = circuits.random_circuit(40, 23, 64, 2, rng, kinds=ALL_KINDS)
+    got, stats = run_gpu(40, g, 64, initial_buckets=1 << 12)
+    o = SparseOracle(64, threads=SparseOracle.max_threads())
+    o.apply(g)
+    assert_identical(got, o.state(sorted=True))
+    assert stats["buckets"] > 1 << 20 and stats["replays"] > 0
+
+
 @pytest.mark.parametrize("name", golden_cases()[1])
 def test_golden_reference_fixtures(name):
     d, _ = golden_cases()
