@@ -154,6 +154,26 @@ int sqc_norm2(sqc_state* st, double* norm2);
  * fidelity = |<b|a>|^2 / (<a|a><b|b>), max_abs_err = max over keys of |a_k - b_k|. */
 int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_err);
 
+/* ---- gate application without allocation ---------------------------------------------- */
+/* No counterpart in the reference. For callers that cannot allocate device memory (a host
+ * application that owns every device allocation, a plugin limited to the buffers it is
+ * handed, code that must not trigger the device-wide synchronization of cudaMalloc/cudaFree):
+ * applies n_gates gates (host array, at most 256) to the sparse FP64 state of nq qubits given
+ * in the caller's DEVICE arrays keys_in/re_in/im_in (n_in distinct keys, at most 16384) and
+ * writes the resulting entries, in no particular order, to the caller's DEVICE arrays
+ * keys_out/re_out/im_out (capacity cap_out); *n_out (host) receives their number. Same
+ * arithmetic, pair rule and pruning as sqc_apply_gates, bit for bit. It calls no
+ * cudaMalloc/cudaFree: the table lives in a fixed device array of about 13 MB, held by every
+ * device that loads the library until exit. At most 14745 groups of 16 consecutive keys may
+ * have been touched during the call (emptied groups included) when a gate pairing keys across
+ * groups runs; beyond that, or when *n_out > cap_out, the call returns SQC_ERR_CAPACITY.
+ * Calls share the array: serialize
+ * calls whose GPU work could overlap. The first call on a device looks up the array's device
+ * address; make it before any stream capture. stream is a cudaStream_t (NULL = default). */
+int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const double* re_in, const double* im_in,
+                    uint64_t n_in, const sqc_gate* gates, uint64_t n_gates, uint64_t* keys_out,
+                    double* re_out, double* im_out, uint64_t cap_out, uint64_t* n_out, void* stream);
+
 /* ---- introspection ------------------------------------------------------------------- */
 typedef struct sqc_stats {
     uint64_t gates_applied;    /* gates executed on the device */

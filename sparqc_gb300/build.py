@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsparqc.so")
-SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_engine.cpp", "sqc_capi.cpp"]
+SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_engine.cpp", "sqc_capi.cpp", "sqc_fixed.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -21,7 +21,7 @@ FP64, FP32 = 64, 32
 EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_state", "sqc_set_state",
            "sqc_apply_gates", "sqc_x", "sqc_y", "sqc_z", "sqc_h", "sqc_phase", "sqc_rz", "sqc_rx", "sqc_ry",
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
-           "sqc_status_string", "sqc_last_error", "sqc_stream")
+           "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed")
 
 
 class HashTableParameters(ctypes.Structure):
