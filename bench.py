@@ -41,8 +41,16 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sparqc", choices=["sparqc", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--circuits", type=int, default=256, help="c4: circuits per batch")
+    ap.add_argument("--autotune", action="store_true", help="c4: autotune the batch before timing")
+    ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
+    ap.add_argument("--rates", type=str, default="10,40", help="c5: arrival rates (circuits/s), comma-separated")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: table memory budget")
+    ap.add_argument("--slice-ms", type=float, default=2.0, help="c5: serving time slice")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--k", type=int, default=None, help="override the workload's branching-qubit count")
+    ap.add_argument("--gates", type=int, default=None, help="override the workload's gate count")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -55,11 +63,18 @@ def dist_env():
     return rank, world, local
 
 
-def workload(name, rank):
+def workload(name, rank, k=None, gates=None):
+    """The named configuration's circuit; k / gates override its size (smaller profiling cases)."""
     from sparqc_gb300 import circuits
-    nq, g = circuits.config_circuit(name, index=rank, seed=0)
-    p = circuits.CONFIGS[name]
-    return nq, g, p
+    p = dict(circuits.CONFIGS[name])
+    if k is None and gates is None:
+        nq, g = circuits.config_circuit(name, index=rank, seed=0)
+        return nq, g, p
+    p["k"] = k if k is not None else p["k"]
+    p["depth"] = gates if gates is not None else p["depth"]
+    rng = circuits.SplitMix64(circuits.stream_seed(name, rank, 0))
+    g = circuits.random_circuit(p["nq"], p["k"], p["depth"], p["max_controls"], rng)
+    return p["nq"], g, p
 
 
 def config_dict(name, p, precision, world):
@@ -151,6 +166,45 @@ def read_profile_traffic():
     return None
 
 
+def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured, precision):
+    """Roofline of the dominant gate-pass kernel over the timed steps.
+
+    Every pass is bracketed by CUDA events on the engine's stream (time_passes); pair passes
+    (one direct_kernel<T, true> launch, or resolve_kernel + staged_kernel<T, true> on large
+    tables) and stream passes (direct/staged_kernel<T, false>) are timed apart. achieved =
+    the kind's algorithmic bytes (device counter) / its event time.
+    """
+    t_pair = (s1["pass_ns_pair"] - s0["pass_ns_pair"]) / 1e9
+    t_stream = (s1["pass_ns_stream"] - s0["pass_ns_stream"]) / 1e9
+    n_pair = (s1["passes_pair"] - s0["passes_pair"]) / steps
+    n_all = (s1["passes"] - s0["passes"]) / steps
+    staged = s1["buckets"] > (1 << 20)
+    T = "double" if precision == 64 else "float"
+    kinds = {
+        "pair": {"kernel": (f"resolve_kernel + staged_kernel<{T}, true>" if staged else f"direct_kernel<{T}, true>"),
+                 "bytes": alg_pair_step * steps, "t": t_pair, "passes": n_pair},
+        "stream": {"kernel": f"staged_kernel<{T}, false>" if staged else f"direct_kernel<{T}, false>",
+                   "bytes": (alg_step - alg_pair_step) * steps, "t": t_stream, "passes": n_all - n_pair},
+    }
+    dom = max(kinds, key=lambda k: kinds[k]["t"])
+    d = kinds[dom]
+    achieved = d["bytes"] / d["t"] / 1e9 if d["t"] > 0 else 0.0
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "traffic": read_profile_traffic(), "kernel": d["kernel"],
+           "launches_per_step": d["passes"] * (2 if (staged and dom == "pair") else 1),
+           "alg_bytes_per_pass": d["bytes"] / steps / max(d["passes"], 1),
+           "avg_pass_us": 1e6 * d["t"] / steps / max(d["passes"], 1),
+           "share_of_step_time": d["t"] * 1e3 / dev_ms if dev_ms > 0 else None,
+           "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs), of measured" if measured
+                           else "fallback 6.8 TB/s, of fallback"),
+           "whole_step_achieved": alg_step * steps / (dev_ms / 1e3) / 1e9}
+    other = "stream" if dom == "pair" else "pair"
+    o = kinds[other]
+    out["other_kernel"] = {"kernel": o["kernel"], "achieved": o["bytes"] / o["t"] / 1e9 if o["t"] > 0 else 0.0,
+                           "share_of_step_time": o["t"] * 1e3 / dev_ms if dev_ms > 0 else None}
+    return out
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -163,7 +217,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    nq, gates, p = workload(args.workload, 0)
+    nq, gates, p = workload(args.workload, 0, args.k, args.gates)
     from oracle.sparse import SparseOracle
     threads = max(1, SparseOracle.max_threads())
     per_step = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
@@ -196,11 +250,14 @@ def run_gpu(args):
     from sparqc_gb300 import build as engine_build, engine
     engine_build.build()
 
-    nq, gates, p = workload(args.workload, rank)
-    stream = torch.cuda.current_stream()
-    A = 16 if args.precision == 64 else 8
+    nq, gates, p = workload(args.workload, rank, args.k, args.gates)
+    # one stream for everything timed: the L2 flush, the events and the engine's kernels
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     st = engine.State(nq, precision=args.precision, stream=stream.cuda_stream,
-                      initial_buckets=1 << max(6, p["k"] - 4 + 1))
+                      initial_buckets=1 << max(6, p["k"] - 4 + 1), time_passes=True)
+    if st.stream != stream.cuda_stream:
+        raise RuntimeError("the engine does not run on the timed stream")
     # warm-up: grows the tables to their final size and fixes the per-step counters
     for _ in range(max(3, args.warmup)):
         sw = st.stats()
@@ -210,6 +267,7 @@ def run_gpu(args):
     s0 = st.stats()
     upd_per_step = s0["amp_updates"]
     alg_per_step = s0["alg_bytes"]
+    alg_pair_step = s0["alg_bytes_pair"]
     passes_per_step = s0["passes"] - sw["passes"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -275,13 +333,8 @@ def run_gpu(args):
         return
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    achieved = alg_per_step * args.steps / t_dev / 1e9
-    traffic = read_profile_traffic()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "kernel": "pass_kernel (gate pass)", "algorithmic_bytes_per_step": alg_per_step,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s",
-                "note": "achieved over the whole step (gate passes are all but one of its kernels)"}
+    roofline = pass_roofline(s0, s1, alg_per_step, alg_pair_step, args.steps, dev_ms, peak, peaks is not None,
+                             args.precision)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(gates, args.cpu_seconds, args.precision)
@@ -296,10 +349,254 @@ def run_gpu(args):
     st.close()
 
 
+# --------------------------------------------------------------------------------------
+# c4: many circuits in one persistent launch (sqc_batch_*), against the plain per-circuit path
+def fidelity(a, b):
+    """|<a|b>|^2 / (<a|a><b|b>) and max |a_k - b_k| of two key-sorted (keys, re, im) states."""
+    ka, kb = a[0], b[0]
+    va = a[1] + 1j * a[2]
+    vb = b[1] + 1j * b[2]
+    common, ia, ib = np.intersect1d(ka, kb, assume_unique=True, return_indices=True)
+    ov = np.vdot(vb[ib], va[ia])
+    na, nb = np.vdot(va, va).real, np.vdot(vb, vb).real
+    diff = np.abs(va[ia] - vb[ib])
+    only_a = np.abs(np.delete(va, ia)) if va.size > ia.size else np.zeros(0)
+    only_b = np.abs(np.delete(vb, ib)) if vb.size > ib.size else np.zeros(0)
+    mx = max([0.0] + [float(x.max()) for x in (diff, only_a, only_b) if x.size])
+    return float(abs(ov) ** 2 / (na * nb)), mx
+
+
+def run_batch(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from sparqc_gb300 import build as engine_build, circuits, engine
+    engine_build.build()
+    cs = [(nq, g) for nq, _, g in circuits.batch_circuits(args.circuits, seed=rank)]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    b = engine.Batch(precision=args.precision, use_graph=True, stream=stream.cuda_stream)
+    b.prepare(cs)
+    tuning = b.autotune() if args.autotune else None
+    for _ in range(max(3, args.warmup)):
+        b.run()
+        b.sync()
+    s0 = b.stats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = s0["kernel_launches"]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local) if rank == 0 else None
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        b.run()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    b.sync()
+    s1 = b.stats()
+    dev_ms = sum(x.elapsed_time(y) for x, y in ev)
+    t = dev_ms / 1e3
+    if world > 1:
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    upd = s1["amp_updates"]
+    value = upd * args.steps * world / t
+    circ_s = len(cs) * args.steps * world / t
+
+    # e2e through the C ABI with host buffers: plan + upload (prepare), run, every state read back
+    e2e_steps = 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(e2e_steps):
+        b.prepare(cs)
+        b.run()
+        b.sync()
+        d2h = 0
+        for i in range(len(cs)):
+            k, r, im = b.state(i, sorted=False)
+            d2h += k.nbytes + r.nbytes + im.nbytes
+    e2e_t = (time.perf_counter() - t0) / e2e_steps
+    h2d = int(sum(g.nbytes for _, g in cs))
+
+    # the plain per-circuit FP64 path on the same circuits: one state per circuit, run alone
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_upd = 0
+    for nq, g in cs:
+        st = engine.State(nq, stream=stream.cuda_stream)
+        st.apply(g)
+        st.sync()
+        plain_upd += st.stats()["amp_updates"]
+        st.close()
+    plain_t = time.perf_counter() - t0
+
+    fid = None
+    if args.precision == 32:
+        b64 = engine.Batch(precision=64, stream=stream.cuda_stream)
+        b64.prepare(cs)
+        b64.run()
+        b64.sync()
+        fs, es = [], []
+        for i in range(len(cs)):
+            f, e = fidelity(b.state(i), b64.state(i))
+            fs.append(f)
+            es.append(e)
+        fid = {"min_fidelity": min(fs), "max_abs_err": max(es), "circuits": len(fs)}
+        b64.close()
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = s1["alg_bytes"] * args.steps / t / 1e9
+    out = {"metric": "amp-updates/s", "value": value, "unit": "amp-updates/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": f"f{args.precision}",
+           "data": "synthetic",
+           "config": {"workload": f"c4: {len(cs)} circuits, qubits 16-48, k 8-18, depth 100-1000, 0-3 controls, "
+                                  f"30/30/40 diag/perm/branch, FP{args.precision}, seed {rank}",
+                      "circuits": len(cs), "precision": f"fp{args.precision}",
+                      "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
+           "circuits_per_s": circ_s,
+           "plain_fp64_per_circuit": {"circuits_per_s": len(cs) / plain_t, "amp_updates_per_s": plain_upd / plain_t,
+                                      "path": "one sqc_create + sqc_apply_gates + sqc_sync per circuit, FP64",
+                                      "speedup_circuits_per_s": circ_s / (len(cs) * world / plain_t)},
+           "e2e": {"value": upd * world / e2e_t, "unit": "amp-updates/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h, "circuits_per_s": len(cs) * world / e2e_t,
+                   "path": "sqc_batch_prepare (host gates) + sqc_batch_run + sqc_batch_get_state for every circuit"},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": None, "kernel": f"batch_run_kernel<{'double' if args.precision == 64 else 'float'}>",
+                        "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs), of measured" if peaks
+                        else "fallback 6.8 TB/s, of fallback"},
+           "fidelity_vs_fp64": fid, "tuning": tuning, "cpu_baseline": None,
+           "gpu_launches": int(s1["kernel_launches"] - launches0), "clocks": clk,
+           "passes_per_step": s1["passes"], "table_bytes": s1["table_bytes"]}
+    print(json.dumps(out), flush=True)
+    b.close()
+
+
+# --------------------------------------------------------------------------------------
+# c5: serving a Poisson arrival stream (sqc_server_*), against the plain per-circuit FP64 path
+def serve_stream(engine, stream, reqs, precision, budget, slice_ms):
+    """Serve reqs [(arrival_s, nq, k, gates)] in wall-clock time. Returns latencies, makespan, stats."""
+    sv = engine.Server(precision=precision, memory_budget=int(budget), slice_ms=slice_ms, stream=stream)
+    n = len(reqs)
+    ids = {}
+    lat = [None] * n
+    i = 0
+    done = 0
+    t0 = time.perf_counter()
+    while done < n:
+        now = time.perf_counter() - t0
+        while i < n and reqs[i][0] <= now:
+            ids[sv.submit(reqs[i][1], reqs[i][3])] = i
+            i += 1
+        st = sv.stats()
+        if st["queued"] == 0 and st["running"] == 0:
+            if i < n:
+                time.sleep(max(0.0, reqs[i][0] - (time.perf_counter() - t0)))
+            continue
+        sv.step()
+        t = time.perf_counter() - t0
+        for rid in sv.completed():
+            j = ids.pop(rid)
+            st, code = sv.status(rid)
+            if code != 0:
+                raise RuntimeError(f"request {j} failed with status {code}")
+            lat[j] = t - reqs[j][0]
+            sv.release(rid)
+            done += 1
+    makespan = time.perf_counter() - t0
+    stats = sv.stats()
+    sv.close()
+    return lat, makespan, stats
+
+
+def run_serve(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from sparqc_gb300 import build as engine_build, circuits, engine
+    engine_build.build()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rates = [float(x) for x in args.rates.split(",")]
+    budget = args.budget_gb * 1e9
+    sweep = []
+    for rate in rates:
+        reqs = circuits.serving_stream(args.requests, rate, seed=rank)
+        lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, args.precision, budget, args.slice_ms)
+        lat = np.array(lat)
+        sweep.append({"rate_per_s": rate, "requests": len(reqs), "circuits_per_s": len(reqs) / makespan,
+                      "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                      "makespan_s": makespan, "amp_updates_per_s": st["amp_updates"] / makespan,
+                      "device_busy_s": st["busy_ms"] / 1e3, "steps": st["steps"],
+                      "large": int(sum(1 for r in reqs if r[1] == 48 and r[2] == 24))})
+    # the plain per-circuit FP64 path over the last stream, back to back (no arrival gaps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _, nq, _, g in reqs:
+        st = engine.State(nq, stream=stream.cuda_stream)
+        st.apply(g)
+        st.sync()
+        st.close()
+    plain_t = time.perf_counter() - t0
+    # fidelity of served results against the plain FP64 path, on a sample (every large circuit
+    # and the first 16 others), served back to back outside the timed runs
+    fid = None
+    if args.precision == 32:
+        sample = [r for r in reqs if r[1] == 48 and r[2] == 24][:4] + [r for r in reqs if r[2] != 24][:16]
+        sv = engine.Server(precision=32, memory_budget=int(budget), slice_ms=args.slice_ms, stream=stream.cuda_stream)
+        rids = [sv.submit(r[1], r[3]) for r in sample]
+        fs, es = [], []
+        while len(fs) < len(rids):
+            sv.step()
+            for rid in sv.completed():
+                r = sample[rids.index(rid)]
+                ref = engine.State(r[1], stream=stream.cuda_stream)
+                ref.apply(r[3])
+                f, e = sv.compare(rid, ref)
+                ref.close()
+                fs.append(f)
+                es.append(e)
+                sv.release(rid)
+        sv.close()
+        fid = {"min_fidelity": min(fs), "max_abs_err": max(es), "circuits": len(fs)}
+    if rank != 0:
+        return
+    best = max(sweep, key=lambda x: x["circuits_per_s"])
+    out = {"metric": "served circuits/s", "value": best["circuits_per_s"], "unit": "circuits/s", "n_gpus": world,
+           "steps": len(rates), "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": f"f{args.precision}", "data": "synthetic",
+           "config": {"workload": f"c5: Poisson arrivals of c4 circuits plus 5% large (48 qubits, k=24, 2000 gates), "
+                                  f"{args.requests} requests per rate, budget {args.budget_gb:g} GB, "
+                                  f"slice {args.slice_ms:g} ms, FP{args.precision}",
+                      "rates": rates, "precision": f"fp{args.precision}"},
+           "sweep": sweep,
+           "plain_fp64_per_circuit": {"circuits_per_s": len(reqs) / plain_t,
+                                      "path": "one sqc_create + sqc_apply_gates + sqc_sync per circuit, FP64, "
+                                              "back to back over the last rate's stream",
+                                      "speedup_circuits_per_s": best["circuits_per_s"] / (len(reqs) / plain_t)},
+           "fidelity_vs_fp64": fid}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c4":
+        run_batch(args)
+    elif args.workload == "c5":
+        run_serve(args)
     else:
         run_gpu(args)
 

@@ -3,7 +3,7 @@
  *
  * The state is a GPU open-addressing hash table mapping 64-bit basis-state keys to complex
  * amplitudes. Gates are applied by pairing each key with k ^ (1 << target), updating the
- * pair with its 2x2 matrix, writing the results into a fresh table and pruning negligible
+ * pair with its 2x2 matrix, writing the results back into the table and pruning negligible
  * amplitudes after branching gates. All entry points take plain pointers and sizes, return
  * an int status (SQC_OK = 0) and never throw.
  *
@@ -90,7 +90,9 @@ typedef struct sqc_options {
     void* stream;              /* cudaStream_t to run on; NULL = the handle creates its own */
     uint32_t device;           /* CUDA device ordinal, default 0 */
     uint32_t max_fused_gates;  /* cap on gates fused into one pass, 0 = default (64) */
-    uint32_t reserved[4];
+    uint32_t time_passes;      /* 1: bracket every gate pass with CUDA events on the handle's stream
+                                  (sqc_stats.pass_ns_*); 0 (default): no events */
+    uint32_t reserved[3];
 } sqc_options;
 
 typedef struct sqc_state sqc_state;
@@ -174,6 +176,142 @@ int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const double* re_in, c
                     uint64_t n_in, const sqc_gate* gates, uint64_t n_gates, uint64_t* keys_out,
                     double* re_out, double* im_out, uint64_t cap_out, uint64_t* n_out, void* stream);
 
+/* ---- many-circuit batch ---------------------------------------------------------------- */
+/* No counterpart in the reference (one state per process, emulator/device/device_data.cuh:36).
+ * A batch runs many independent circuits, each from |0...0>, in one persistent kernel launch:
+ * every circuit gets its own table slice, sized from the number of 16-key groups its gates
+ * can ever produce (known on the host from which qubits its gates can make differ), so no
+ * slice ever grows and the launch needs no host round trip. Each circuit's result is
+ * bit-identical to running it alone through sqc_create/sqc_apply_gates. */
+typedef struct sqc_batch sqc_batch;
+
+typedef struct sqc_circuit_desc {
+    uint32_t nq;              /* qubits, 1..64 */
+    uint32_t reserved;
+    const sqc_gate* gates;    /* host array, read during sqc_batch_prepare only */
+    uint64_t n_gates;
+} sqc_circuit_desc;
+
+typedef struct sqc_batch_options {
+    uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 */
+    uint32_t device;           /* CUDA device ordinal */
+    void* stream;              /* cudaStream_t; NULL = the batch creates its own */
+    double prune_threshold;    /* default 1e-14 */
+    double load_factor;        /* groups per bucket of a slice at the group bound, (0, 0.45]; default 0.45 */
+    uint32_t min_chunk;        /* list entries a warp takes at once, a multiple of 4; default 8 */
+    uint32_t blocks_per_sm;    /* persistent blocks per SM, 0 = as many as fit */
+    uint64_t memory_budget;    /* bytes of device memory the batch may hold, 0 = 98% of the device */
+    uint32_t use_graph;        /* 1: sqc_batch_run replays a captured CUDA graph */
+    uint32_t reserved[5];
+} sqc_batch_options;
+
+/* Tuning picked by sqc_batch_autotune. */
+typedef struct sqc_batch_tuning {
+    double load_factor;
+    uint32_t min_chunk;
+    uint32_t blocks_per_sm;
+    double best_ms;            /* run time of the chosen tuning */
+    double default_ms;         /* run time of the tuning in effect before the call */
+    uint32_t candidates;       /* tunings timed */
+    uint32_t reserved;
+} sqc_batch_tuning;
+
+typedef struct sqc_batch_stats {
+    uint64_t circuits;
+    uint64_t passes;           /* passes completed in the last run */
+    uint64_t amp_updates;      /* sum over circuits and gates of input nonzeros, last run */
+    uint64_t alg_bytes;        /* algorithmic bytes of the passes, last run (sqc_stats.alg_bytes) */
+    uint64_t table_bytes;      /* device bytes of the table slices */
+    uint64_t kernel_launches;  /* kernels launched by the batch so far */
+    double last_run_ms;        /* device time of the last run (CUDA events around its launches) */
+} sqc_batch_stats;
+
+void sqc_batch_default_options(sqc_batch_options* opt);
+int sqc_batch_create(const sqc_batch_options* opt, sqc_batch** out);
+int sqc_batch_destroy(sqc_batch* b);
+/* Plan n circuits, lay out their slices and upload their gates. Replaces any earlier circuits.
+ * SQC_ERR_BUDGET when the slices do not fit the memory budget. */
+int sqc_batch_prepare(sqc_batch* b, const sqc_circuit_desc* circuits, uint32_t n);
+/* Run every circuit from |0...0> to its last gate. Asynchronous; may be called repeatedly. */
+int sqc_batch_run(sqc_batch* b);
+/* Wait for the run. SQC_ERR_STATE if any circuit failed (sqc_batch_circuit_status tells which). */
+int sqc_batch_sync(sqc_batch* b);
+/* Status of circuit i after sync: SQC_OK, or the error that stopped it. */
+int sqc_batch_circuit_status(sqc_batch* b, uint32_t i, int* status);
+int sqc_batch_nnz(sqc_batch* b, uint32_t i, uint64_t* nnz);
+/* Readout of circuit i, as sqc_get_state. */
+int sqc_batch_get_state(sqc_batch* b, uint32_t i, uint64_t* keys, double* re, double* im, uint64_t cap,
+                        uint64_t* n, uint32_t flags);
+/* Time candidate tunings (load factor, chunk size, blocks per SM) on the prepared circuits and
+ * keep the fastest. Runs the batch several times; the circuits' states afterwards are those
+ * of a complete run. */
+int sqc_batch_autotune(sqc_batch* b, sqc_batch_tuning* out);
+int sqc_batch_get_stats(sqc_batch* b, sqc_batch_stats* out);
+/* Compare circuit i of a synced batch with a state of the same qubit count, as sqc_compare
+ * (fidelity and max |a_k - b_k|, on the device, FP64 accumulation). The state is synced first. */
+int sqc_batch_compare(sqc_batch* b, uint32_t i, sqc_state* ref, double* fidelity, double* max_abs_err);
+const char* sqc_batch_last_error(sqc_batch* b);
+void* sqc_batch_stream(sqc_batch* b);
+
+/* ---- serving loop ---------------------------------------------------------------------- */
+/* No counterpart in the reference. Circuits arrive one by one (sqc_server_submit) and are
+ * admitted into resident slots while others run: each sqc_server_step admits the queued
+ * requests whose table slices fit the memory budget (first come, first served), then runs one
+ * time slice of the same persistent kernel as the batch over every resident circuit: circuits
+ * that finish leave, the others park at a pass boundary when the slice ends and continue in
+ * the next step. States stay on the device between steps and after completion until released.
+ * A request's result is bit-identical to running its circuit alone. */
+typedef struct sqc_server sqc_server;
+
+typedef struct sqc_server_options {
+    uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 */
+    uint32_t device;
+    void* stream;              /* cudaStream_t; NULL = the server creates its own */
+    double prune_threshold;    /* default 1e-14 */
+    double load_factor;        /* as sqc_batch_options, default 0.45 */
+    uint64_t memory_budget;    /* bytes of device memory for slices and gates, 0 = 120 GB (at most 90% of the device) */
+    uint32_t max_slots;        /* circuits resident at once, default 1024 */
+    uint32_t min_chunk;        /* default 8 */
+    double slice_ms;           /* device time of one step before running circuits park, default 2 */
+    uint32_t reserved[6];
+} sqc_server_options;
+
+enum { SQC_REQ_QUEUED = 0, SQC_REQ_RUNNING = 1, SQC_REQ_DONE = 2 };
+
+typedef struct sqc_server_stats {
+    uint64_t queued, running, completed;   /* requests in each state (completed: not yet released) */
+    uint64_t steps;                        /* steps that launched work */
+    uint64_t kernel_launches;
+    uint64_t amp_updates;                  /* of the requests completed so far */
+    uint64_t pool_bytes, pool_used;        /* the memory budget and its part in use */
+    double busy_ms;                        /* device time of all steps (CUDA events) */
+} sqc_server_stats;
+
+void sqc_server_default_options(sqc_server_options* opt);
+int sqc_server_create(const sqc_server_options* opt, sqc_server** out);
+int sqc_server_destroy(sqc_server* s);
+/* Plan a circuit (from |0...0>) and queue it; *id receives the request id. SQC_ERR_BUDGET if
+ * the circuit could never fit the memory budget. */
+int sqc_server_submit(sqc_server* s, const sqc_circuit_desc* circuit, uint64_t* id);
+/* Admit what fits, run one time slice, wait for it. *finished (may be NULL) receives the number
+ * of requests that completed during the step. */
+int sqc_server_step(sqc_server* s, uint32_t* finished);
+/* Ids of completed, unreleased requests (up to cap, oldest first); *n receives their number. */
+int sqc_server_completed(sqc_server* s, uint64_t* ids, uint32_t cap, uint32_t* n);
+/* state: SQC_REQ_*; status: SQC_OK or the error that stopped the request. */
+int sqc_server_request_status(sqc_server* s, uint64_t id, int* state, int* status);
+int sqc_server_nnz(sqc_server* s, uint64_t id, uint64_t* nnz);
+/* Readout of a completed request, as sqc_get_state. */
+int sqc_server_get_state(sqc_server* s, uint64_t id, uint64_t* keys, double* re, double* im, uint64_t cap,
+                         uint64_t* n, uint32_t flags);
+/* Free the slot and memory of a completed request. */
+int sqc_server_release(sqc_server* s, uint64_t id);
+int sqc_server_get_stats(sqc_server* s, sqc_server_stats* out);
+/* Compare a completed request with a state of the same qubit count, as sqc_compare. */
+int sqc_server_compare(sqc_server* s, uint64_t id, sqc_state* ref, double* fidelity, double* max_abs_err);
+const char* sqc_server_last_error(sqc_server* s);
+void* sqc_server_stream(sqc_server* s);
+
 /* ---- introspection ------------------------------------------------------------------- */
 typedef struct sqc_stats {
     uint64_t gates_applied;    /* gates executed on the device */
@@ -186,6 +324,12 @@ typedef struct sqc_stats {
     uint64_t alg_bytes;        /* algorithmic bytes of the passes: (nnz_in + nnz_out) * (8 + A) per
                                   key-changing pass, nnz * (8 + 2A) per pass that keeps every key;
                                   A = 16 (FP64) or 8 (FP32). Since the last reset, after sync. */
+    uint64_t alg_bytes_pair;   /* the part of alg_bytes moved by pair passes (a gate pairing keys of
+                                  different 16-key groups, plus the gates fused after it) */
+    uint64_t passes_pair;      /* pair passes among `passes` */
+    uint64_t pass_ns_pair;     /* device time of the pair passes, from CUDA events (time_passes = 1;
+                                  since creation, after sync) */
+    uint64_t pass_ns_stream;   /* device time of the other passes, likewise */
 } sqc_stats;
 
 int sqc_get_stats(sqc_state* st, sqc_stats* out);

@@ -14,7 +14,12 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsparqc.so")
-SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_engine.cpp", "sqc_capi.cpp", "sqc_fixed.cu"]
+SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_batch.cu", "sqc_engine.cpp", "sqc_plan.cpp", "sqc_batch.cpp",
+           "sqc_serve.cpp",
+           "sqc_capi.cpp", "sqc_capi_batch.cpp", "sqc_fixed.cu"]
+# per-file extra flags: the persistent batch kernel reads data other SMs wrote during the
+# same launch, so its global loads default to L2 (L1 is not coherent across SMs)
+EXTRA = {"sqc_batch.cu": ["-Xptxas", "-dlcm=cg"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -51,8 +56,8 @@ def build(force=False, verbose=False):
     objs = []
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
-        cmd = [cc] + _flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(OUT_DIR, src.replace(".", "_") + ".o")
+        cmd = [cc] + _flags() + EXTRA.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -5,11 +5,7 @@
 #include <string>
 
 #include "../../include/sparqc.h"
-#include "sqc_engine.h"
-
-struct sqc_state {
-    sqc::Engine eng;
-};
+#include "sqc_handles.h"
 
 namespace {
 
@@ -51,7 +47,8 @@ void sqc_default_options(sqc_options* opt) {
     opt->stream = nullptr;
     opt->device = 0;
     opt->max_fused_gates = 0;
-    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
+    opt->time_passes = 0;
+    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt, sqc_state** out) {

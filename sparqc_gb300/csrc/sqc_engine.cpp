@@ -24,15 +24,6 @@ unsigned long long pow2_at_least(unsigned long long x) {
     return p;
 }
 
-bool is_diag_kind(uint32_t k) {
-    return k == KZ || k == KPHASE || k == KRZ || k == KS || k == KSDG || k == KT || k == KTDG || k == KYPH;
-}
-bool is_one_sided_kind(uint32_t k) {
-    return k == KZ || k == KPHASE || k == KS || k == KSDG || k == KT || k == KTDG;
-}
-bool is_branch_kind(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
-bool is_swap_kind(uint32_t k) { return k == KX || k == KY; }
-bool streamable(const GateDesc& d) { return d.target < (uint32_t)kSlotBits || is_diag_kind(d.kind); }
 
 }  // namespace
 
@@ -46,6 +37,7 @@ Engine::~Engine() {
     if (d_rk_) cudaFree(d_rk_);
     if (d_rr_) cudaFree(d_rr_);
     if (d_ri_) cudaFree(d_ri_);
+    for (cudaEvent_t e : ev_all_) cudaEventDestroy(e);
     if (own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -86,6 +78,7 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     thr_ = o.prune_threshold;
     lf_ = o.load_factor;
     max_run_ = o.max_fused_gates ? std::min<uint32_t>(o.max_fused_gates, kMaxRun) : kMaxRun;
+    time_passes_ = o.time_passes != 0;
     device_ = (int)o.device;
 
     int ndev = 0;
@@ -194,66 +187,7 @@ int Engine::ensure_readout(size_t n) {
     return SQC_OK;
 }
 
-// Descriptor of one device gate in the stored-key frame, coefficients resolved on the host.
-GateDesc Engine::make_desc(uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g) const {
-    GateDesc d;
-    std::memset(&d, 0, sizeof d);
-    d.kind = kind;
-    d.target = target;
-    d.ctrl = ctrl;
-    d.cval = ctrl & ~plan_.frame;
-    d.flip = (uint32_t)((plan_.frame >> target) & 1ULL);
-    switch (kind) {
-    case KPHASE: d.c = std::cos(g.theta); d.s = std::sin(g.theta); break;
-    case KRZ: case KRX: case KRY: {
-        const double h = g.theta / 2.;   // the reference passes par/2 (table_manager.cuh:333-336)
-        d.c = std::cos(h);
-        d.s = std::sin(h);
-        break;
-    }
-    case KT: d.c = 0.70710678118654752440; d.s = 0.70710678118654752440; break;
-    case KTDG: d.c = 0.70710678118654752440; d.s = -0.70710678118654752440; break;
-    case KH: d.c = 1. / std::sqrt(2.); break;   // as in h_core (device_data.cuh:205)
-    case KU: {
-        const double c = std::cos(g.theta / 2.), s = std::sin(g.theta / 2.);
-        const double cl = std::cos(g.lambda), sl = std::sin(g.lambda);
-        const double cp = std::cos(g.phi), sp = std::sin(g.phi);
-        const double cpl = std::cos(g.phi + g.lambda), spl = std::sin(g.phi + g.lambda);
-        d.m[0] = c;         d.m[1] = 0.;
-        d.m[2] = -(cl * s); d.m[3] = -(sl * s);
-        d.m[4] = cp * s;    d.m[5] = sp * s;
-        d.m[6] = cpl * c;   d.m[7] = spl * c;
-        break;
-    }
-    default: break;
-    }
-    d.cf = (float)d.c;
-    d.sf = (float)d.s;
-    for (int i = 0; i < 8; ++i) d.mf[i] = (float)d.m[i];
-    return d;
-}
-
-// Resolve one gate against what the host knows of the keys. Returns true and a descriptor
-// when the gate needs the device; otherwise the gate was applied here (identity, or an
-// uncontrolled X as a frame flip) and is credited to the next device gate.
-bool Engine::plan_gate(const sqc_gate& g, GateDesc* out) {
-    Planner& p = plan_;
-    const unsigned long long bq = 1ULL << g.target;
-    const unsigned long long kc = g.controls & p.kmask;
-    if ((p.kval & kc) != kc) { ++p.credit; return false; }   // a control is known to be 0
-    const unsigned long long ctrl = g.controls & ~p.kmask;   // controls still to test per key
-    if (is_swap_kind(g.kind) && ctrl == 0) {
-        p.frame ^= bq;
-        if (p.kmask & bq) p.kval ^= bq;
-        if (g.kind == KX) { ++p.credit; return false; }
-        *out = make_desc(KYPH, g.target, 0, g);   // Y = relabel + diag(-i, +i)
-        return true;
-    }
-    if (is_one_sided_kind(g.kind) && (p.kmask & bq) && !(p.kval & bq)) { ++p.credit; return false; }
-    *out = make_desc(g.kind, g.target, ctrl, g);
-    if (is_branch_kind(g.kind) || is_swap_kind(g.kind)) p.kmask &= ~bq;
-    return true;
-}
+bool Engine::plan_gate(const sqc_gate& g, GateDesc* out) { return sqc::plan_gate(plan_, g, out); }
 
 int Engine::set_zero() {
     pending_.clear();
@@ -327,11 +261,7 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
 int Engine::apply(const sqc_gate* gates, uint64_t n) {
     if (n && !gates) return fail(SQC_ERR_ARG, "null gate array");
     for (uint64_t i = 0; i < n; ++i) {
-        const sqc_gate& g = gates[i];
-        if (g.kind > SQC_U) return fail(SQC_ERR_ARG, "unknown gate kind");
-        if (g.target >= nq_) return fail(SQC_ERR_ARG, "target qubit out of range");
-        if (nq_ < 64 && (g.controls >> nq_)) return fail(SQC_ERR_ARG, "control qubit out of range");
-        if ((g.controls >> g.target) & 1ULL) return fail(SQC_ERR_ARG, "target qubit among the controls");
+        if (const char* why = check_gate(gates[i], nq_)) return fail(SQC_ERR_ARG, why);
     }
     pending_.insert(pending_.end(), gates, gates + n);
     if (pending_.size() >= kFlushAt) return flush();
@@ -382,6 +312,8 @@ int Engine::flush() {
     a.amp_bytes = dbl_ ? 16u : 8u;
     a.max_groups = max_groups();
     a.prune = prune_;
+    cudaEvent_t ev_prev = nullptr;
+    if (time_passes_ && (rc = record_event(&ev_prev))) return rc;
     size_t i = 0;
     while (i < nd) {
         const size_t start = i;
@@ -398,6 +330,13 @@ int Engine::flush() {
         a.range = pass_range(list_hint_, sms_);
         const int nl = launch_pass(a, list_hint_, dbl_, sms_, stream_);
         if (nl < 0) return cuda(cudaGetLastError(), "gate pass");
+        if (time_passes_) {
+            cudaEvent_t ev = nullptr;
+            if ((rc = record_event(&ev))) return rc;
+            timed_.push_back(TimedPass{ev_prev, ev, pair});
+            ev_prev = ev;
+        }
+        passes_pair_ += pair ? 1 : 0;
         passes_.push_back(PassRec{snap_log_, snap_plan_});
         snap_log_ = src[i - 1] + 1;
         snap_plan_ = after[i - 1];
@@ -412,7 +351,49 @@ int Engine::read_ctl() {
     int rc;
     if ((rc = cuda(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_), "D2H ctl")))
         return rc;
-    return cuda(cudaStreamSynchronize(stream_), "sync");
+    if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
+    harvest_events();
+    return SQC_OK;
+}
+
+// Record an event on the stream (from the free list, or a new one).
+int Engine::record_event(cudaEvent_t* out) {
+    cudaEvent_t e;
+    if (!ev_free_.empty()) {
+        e = ev_free_.back();
+        ev_free_.pop_back();
+    } else {
+        int rc;
+        if ((rc = cuda(cudaEventCreate(&e), "event create"))) return rc;
+        ev_all_.push_back(e);
+    }
+    *out = e;
+    return cuda(cudaEventRecord(e, stream_), "event record");
+}
+
+// After a stream synchronize: add the timed passes to the totals and recycle their events.
+// An event that starts one pass and ends the previous one is recycled once.
+void Engine::harvest_events() {
+    if (timed_.empty()) return;
+    for (const TimedPass& p : timed_) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.before, p.after) == cudaSuccess) {
+            const uint64_t ns = (uint64_t)((double)ms * 1e6);
+            if (p.pair) pass_ns_pair_ += ns;
+            else pass_ns_stream_ += ns;
+        }
+    }
+    std::vector<cudaEvent_t> used;
+    used.reserve(2 * timed_.size());
+    for (const TimedPass& p : timed_) {
+        used.push_back(p.before);
+        used.push_back(p.after);
+    }
+    std::sort(used.begin(), used.end());
+    used.erase(std::unique(used.begin(), used.end()), used.end());
+    ev_free_.insert(ev_free_.end(), used.begin(), used.end());
+    timed_.clear();
+    cudaGetLastError();
 }
 
 int Engine::sync() {
@@ -572,16 +553,24 @@ int Engine::norm2(double* out) {
 }
 
 int Engine::compare(Engine& b, double* fidelity, double* max_abs_err) {
-    if (b.nq_ != nq_) return fail(SQC_ERR_ARG, "states differ in qubit count");
-    if (b.device_ != device_) return fail(SQC_ERR_ARG, "states live on different devices");
     int rc;
     if ((rc = b.sync())) return fail(rc, "compare: " + b.err);
+    return compare_with(b.dev(), b.ctl_, b.list_hint_, b.dbl_, b.plan_.frame, b.nq_, b.device_, fidelity,
+                        max_abs_err);
+}
+
+int Engine::compare_with(const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
+                         unsigned long long frame_b, uint32_t nq_b, int device_b, double* fidelity,
+                         double* max_abs_err) {
+    if (nq_b != nq_) return fail(SQC_ERR_ARG, "states differ in qubit count");
+    if (device_b != device_) return fail(SQC_ERR_ARG, "states live on different devices");
+    int rc;
     if ((rc = sync())) return rc;
     if ((rc = cuda(cudaMemsetAsync(ctl_->acc, 0, sizeof(ctl_->acc), stream_), "memset")) ||
         (rc = cuda(cudaMemsetAsync(&ctl_->acc_max, 0, sizeof(unsigned long long), stream_), "memset")))
         return rc;
-    if ((rc = cuda(launch_compare(dev(), ctl_, list_hint_, dbl_, b.dev(), b.ctl_, b.list_hint_, b.dbl_,
-                                  plan_.frame ^ b.plan_.frame, ctl_, sms_, stream_),
+    if ((rc = cuda(launch_compare(dev(), ctl_, list_hint_, dbl_, tb, cb, std::max<unsigned long long>(hint_b, 1),
+                                  dbl_b, plan_.frame ^ frame_b, ctl_, sms_, stream_),
                    "compare")))
         return rc;
     launches_ += 2;
@@ -605,6 +594,10 @@ int Engine::stats(sqc_stats* out) {
     out->replays = replays_;
     out->amp_updates = (ctl_host_ ? ctl_host_->amp_updates : 0) + host_upd_;
     out->alg_bytes = ctl_host_ ? ctl_host_->alg_bytes : 0;
+    out->alg_bytes_pair = ctl_host_ ? ctl_host_->alg_bytes_pair : 0;
+    out->passes_pair = passes_pair_;
+    out->pass_ns_pair = pass_ns_pair_;
+    out->pass_ns_stream = pass_ns_stream_;
     return SQC_OK;
 }
 

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sparqc.h"
+#include "sqc_plan.h"
 #include "sqc_types.h"
 
 namespace sqc {
@@ -21,17 +22,6 @@ struct HostTable {
     Unit* units = nullptr;
     unsigned int* counts = nullptr;
     unsigned long long nb = 0;
-};
-
-// What the host knows about the keys without looking at them: stored key = actual key ^
-// frame; bits in kmask are identical across all keys and equal kval. Gates whose effect
-// follows from this are resolved here: an uncontrolled X flips a frame bit, a gate with a
-// known-zero control or a one-sided diagonal gate on a known-zero bit is the identity.
-struct Planner {
-    unsigned long long frame = 0;
-    unsigned long long kmask = ~0ULL;
-    unsigned long long kval = 0;
-    uint32_t credit = 0;   // resolved gates not yet credited to a device gate
 };
 
 struct PassRec {
@@ -56,9 +46,14 @@ public:
     int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
     int norm2(double* out);
     int compare(Engine& b, double* fidelity, double* max_abs_err);
+    // Compare this state (a) with a table that another object owns (b, on the same device,
+    // not being modified), of nb_hint live buckets, precision dbl_b and key frame frame_b.
+    int compare_with(const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
+                     unsigned long long frame_b, uint32_t nq_b, int device_b, double* fidelity, double* max_abs_err);
     int stats(sqc_stats* out);
     cudaStream_t stream() const { return stream_; }
     uint32_t nq() const { return nq_; }
+    int device() const { return device_; }
 
     std::string err;
 
@@ -74,8 +69,9 @@ private:
     int ensure_desc(size_t n);
     int ensure_readout(size_t n);
     bool plan_gate(const sqc_gate& g, GateDesc* out);
-    GateDesc make_desc(uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g) const;
     int read_ctl();
+    int record_event(cudaEvent_t* out);
+    void harvest_events();
     unsigned long long max_groups() const;
 
     int device_ = 0;
@@ -115,6 +111,19 @@ private:
     size_t rcap_ = 0;
 
     uint64_t gates_applied_ = 0, passes_run_ = 0, launches_ = 0, replays_ = 0, rebuilds_ = 0;
+    uint64_t passes_pair_ = 0;
+
+    // pass timing (time_passes): an event before the first pass of a flush and one after every
+    // pass; each timed pass spans [before, after], the after event of the pass before it being
+    // its before event
+    struct TimedPass {
+        cudaEvent_t before, after;
+        bool pair;
+    };
+    bool time_passes_ = false;
+    std::vector<cudaEvent_t> ev_free_, ev_all_;
+    std::vector<TimedPass> timed_;
+    uint64_t pass_ns_pair_ = 0, pass_ns_stream_ = 0;
 };
 
 }  // namespace sqc

@@ -56,6 +56,7 @@ __global__ void set_zero_kernel(TableDev t, Ctl* ctl, int dbl) {
         ctl->seq = 0;
         ctl->amp_updates = 0;
         ctl->alg_bytes = 0;
+        ctl->alg_bytes_pair = 0;
         bool created;
         sb = claim_group(t, ctl->epoch, 0ULL, &ctl->status, &created);
     }
@@ -87,6 +88,7 @@ __global__ void set_state_begin_kernel(Ctl* ctl) {
     ctl->seq = 0;
     ctl->amp_updates = 0;
     ctl->alg_bytes = 0;
+    ctl->alg_bytes_pair = 0;
     ctl->out_count = 0;
     ctl->list_n = ctl->list_tail = 0;
     ctl->nnz = 0;

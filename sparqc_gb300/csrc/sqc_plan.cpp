@@ -1,0 +1,80 @@
+// Host-side gate planning: see sqc_plan.h.
+#include "sqc_plan.h"
+
+#include <cmath>
+#include <cstring>
+
+namespace sqc {
+
+const char* check_gate(const sqc_gate& g, uint32_t nq) {
+    if (g.kind > SQC_U) return "unknown gate kind";
+    if (g.target >= nq) return "target qubit out of range";
+    if (nq < 64 && (g.controls >> nq)) return "control qubit out of range";
+    if ((g.controls >> g.target) & 1ULL) return "target qubit among the controls";
+    return nullptr;
+}
+
+GateDesc make_desc(const Planner& p, uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g) {
+    GateDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.kind = kind;
+    d.target = target;
+    d.ctrl = ctrl;
+    d.cval = ctrl & ~p.frame;
+    d.flip = (uint32_t)((p.frame >> target) & 1ULL);
+    switch (kind) {
+    case KPHASE: d.c = std::cos(g.theta); d.s = std::sin(g.theta); break;
+    case KRZ: case KRX: case KRY: {
+        const double h = g.theta / 2.;   // the reference passes par/2 (table_manager.cuh:333-336)
+        d.c = std::cos(h);
+        d.s = std::sin(h);
+        break;
+    }
+    case KT: d.c = 0.70710678118654752440; d.s = 0.70710678118654752440; break;
+    case KTDG: d.c = 0.70710678118654752440; d.s = -0.70710678118654752440; break;
+    case KH: d.c = 1. / std::sqrt(2.); break;   // as in h_core (device_data.cuh:205)
+    case KU: {
+        const double c = std::cos(g.theta / 2.), s = std::sin(g.theta / 2.);
+        const double cl = std::cos(g.lambda), sl = std::sin(g.lambda);
+        const double cp = std::cos(g.phi), sp = std::sin(g.phi);
+        const double cpl = std::cos(g.phi + g.lambda), spl = std::sin(g.phi + g.lambda);
+        d.m[0] = c;         d.m[1] = 0.;
+        d.m[2] = -(cl * s); d.m[3] = -(sl * s);
+        d.m[4] = cp * s;    d.m[5] = sp * s;
+        d.m[6] = cpl * c;   d.m[7] = spl * c;
+        break;
+    }
+    default: break;
+    }
+    d.cf = (float)d.c;
+    d.sf = (float)d.s;
+    for (int i = 0; i < 8; ++i) d.mf[i] = (float)d.m[i];
+    return d;
+}
+
+bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out) {
+    const unsigned long long bq = 1ULL << g.target;
+    const unsigned long long kc = g.controls & p.kmask;
+    if ((p.kval & kc) != kc) { ++p.credit; return false; }   // a control is known to be 0
+    const unsigned long long ctrl = g.controls & ~p.kmask;   // controls still to test per key
+    if (is_swap_kind(g.kind) && ctrl == 0) {
+        p.frame ^= bq;
+        if (p.kmask & bq) p.kval ^= bq;
+        if (g.kind == KX) { ++p.credit; return false; }
+        *out = make_desc(p, KYPH, g.target, 0, g);   // Y = relabel + diag(-i, +i)
+        return true;
+    }
+    if (is_one_sided_kind(g.kind) && (p.kmask & bq) && !(p.kval & bq)) { ++p.credit; return false; }
+    *out = make_desc(p, g.kind, g.target, ctrl, g);
+    if (is_branch_kind(g.kind) || is_swap_kind(g.kind)) p.kmask &= ~bq;
+    return true;
+}
+
+unsigned long long group_bound(const Planner& p, uint32_t nq) {
+    const unsigned long long reg = nq >= 64 ? ~0ULL : ((1ULL << nq) - 1);
+    const unsigned long long var = ~p.kmask & reg & ~15ULL;
+    const int bits = __builtin_popcountll(var);
+    return bits >= 63 ? (1ULL << 63) : (1ULL << bits);
+}
+
+}  // namespace sqc

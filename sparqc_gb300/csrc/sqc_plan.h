@@ -1,0 +1,68 @@
+// Host-side gate planning shared by the single-state engine and the many-circuit batch:
+// resolution of gates against what is known about the keys, descriptor construction
+// (coefficients on the host) and the split of a descriptor sequence into passes.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/sparqc.h"
+#include "sqc_types.h"
+
+namespace sqc {
+
+// What the host knows about the keys without looking at them: stored key = actual key ^
+// frame; bits in kmask are identical across all keys and equal kval. Gates whose effect
+// follows from this are resolved here: an uncontrolled X flips a frame bit, a gate with a
+// known-zero control or a one-sided diagonal gate on a known-zero bit is the identity.
+// kmask only loses bits, so ~kmask is every bit that has ever differed between keys.
+struct Planner {
+    unsigned long long frame = 0;
+    unsigned long long kmask = ~0ULL;
+    unsigned long long kval = 0;
+    uint32_t credit = 0;   // resolved gates not yet credited to a device gate
+};
+
+inline bool is_diag_kind(uint32_t k) {
+    return k == KZ || k == KPHASE || k == KRZ || k == KS || k == KSDG || k == KT || k == KTDG || k == KYPH;
+}
+inline bool is_one_sided_kind(uint32_t k) {
+    return k == KZ || k == KPHASE || k == KS || k == KSDG || k == KT || k == KTDG;
+}
+inline bool is_branch_kind(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
+inline bool is_swap_kind(uint32_t k) { return k == KX || k == KY; }
+// A gate that never pairs keys of different 16-key groups.
+inline bool streamable(const GateDesc& d) { return d.target < (uint32_t)kSlotBits || is_diag_kind(d.kind); }
+
+// Check one gate against a register of nq qubits; nullptr when valid, else the reason.
+const char* check_gate(const sqc_gate& g, uint32_t nq);
+
+// Descriptor of one device gate in the stored-key frame of p, coefficients resolved here.
+GateDesc make_desc(const Planner& p, uint32_t kind, uint32_t target, unsigned long long ctrl, const sqc_gate& g);
+
+// Resolve one gate against p. Returns true and a descriptor when the gate needs the device;
+// otherwise the gate was applied here (identity, or an uncontrolled X as a frame flip) and
+// is counted in p.credit, to be credited to the next device gate.
+bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out);
+
+// Passes of a descriptor sequence: either a run of at most max_run streamable gates, or one
+// cross-group gate followed by such a run. f(g0, g1, pair, keys_fixed) is called per pass.
+template <class F>
+void split_passes(const GateDesc* d, size_t n, size_t max_run, F&& f) {
+    size_t i = 0;
+    while (i < n) {
+        const size_t start = i;
+        const bool pair = !streamable(d[i]);
+        if (pair) ++i;
+        while (i < n && i - start < max_run && streamable(d[i])) ++i;
+        bool fixed = true;
+        for (size_t k = start; k < i; ++k) fixed = fixed && is_diag_kind(d[k].kind);
+        f(start, i, pair, fixed);
+    }
+}
+
+// Largest number of 16-key groups a state can ever hold while running a gate sequence whose
+// planning ended in p (starting from keys that agreed on every bit of the starting kmask):
+// 2^(bits >= 4 that have ever differed between keys).
+unsigned long long group_bound(const Planner& p, uint32_t nq);
+
+}  // namespace sqc

@@ -1,0 +1,111 @@
+// Serving loop: circuits arrive one at a time and share the GPU with those already running.
+//
+// A request is planned on submit (as a batch circuit). A step admits queued requests in
+// arrival order while a slot is free and their table slice plus gate descriptors fit the
+// memory pool, then launches the batch kernel over every resident slot with a deadline: new
+// requests start from |0...0>, parked ones resume, and every circuit whose pass ends after the
+// deadline parks again. The step waits for the launch and retires the circuits that finished.
+// Their states stay resident until released.
+#pragma once
+#include <cstdint>
+#include <deque>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/sparqc.h"
+#include "sqc_batch.h"
+#include "sqc_pool.h"
+
+namespace sqc {
+
+class Server {
+public:
+    Server() = default;
+    ~Server();
+    Server(const Server&) = delete;
+    Server& operator=(const Server&) = delete;
+
+    int init(const sqc_server_options* opt);
+    int submit(const sqc_circuit_desc* c, uint64_t* id);
+    int step(uint32_t* finished);
+    int completed(uint64_t* ids, uint32_t cap, uint32_t* n);
+    int request_status(uint64_t id, int* state, int* status);
+    int nnz(uint64_t id, uint64_t* out);
+    int get_state(uint64_t id, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
+    int release(uint64_t id);
+    int stats(sqc_server_stats* out);
+    cudaStream_t stream() const { return stream_; }
+    int device() const { return device_; }
+    // Table, device control block, live-bucket count, key frame, qubits and precision of a
+    // completed request (for comparisons against another state).
+    int table_of(uint64_t id, TableDev* t, const Ctl** ctl, unsigned long long* hint, unsigned long long* frame,
+                 uint32_t* nq, bool* dbl);
+
+    std::string err;
+
+private:
+    struct Request {
+        CircuitPlan plan;
+        int state = SQC_REQ_QUEUED;
+        int status = SQC_OK;
+        int slot = -1;
+        size_t off = 0, bytes = 0;   // pool block (slice, then descriptors and passes)
+        unsigned long long nb = 0;
+        TableDev table{};
+        Ctl ctl{};                   // control block copied back when the request completed
+    };
+
+    int fail(int code, const std::string& msg);
+    int cuda(cudaError_t e, const char* what);
+    size_t request_bytes(const Request& r) const;
+    int admit();
+    BatchArgs args(uint32_t n) const;
+
+    int device_ = 0;
+    int sms_ = 1;
+    bool dbl_ = true;
+    PruneBits prune_{};
+    double lf_ = 0.45;
+    uint32_t min_chunk_ = 8;
+    uint32_t max_slots_ = 1024;
+    double slice_ms_ = 2.0;
+    cudaStream_t stream_ = nullptr;
+    bool own_stream_ = false;
+
+    unsigned char* pool_ = nullptr;
+    RangePool alloc_;
+    BCirc* d_circ_ = nullptr;
+    Ctl* d_ctl_ = nullptr;
+    BSched* d_sched_ = nullptr;
+    unsigned long long* d_words_ = nullptr;
+    unsigned* d_cmd_ = nullptr;
+    unsigned* d_limit_ = nullptr;
+    BatchCtl* d_bctl_ = nullptr;
+    BCirc* h_circ_ = nullptr;     // pinned mirrors
+    Ctl* h_ctl_ = nullptr;
+    BSched* h_sched_ = nullptr;
+    unsigned* h_cmd_ = nullptr;
+    unsigned* h_limit_ = nullptr;
+    BatchCtl* h_bctl_ = nullptr;
+
+    std::vector<uint64_t> slot_req_;     // request id per slot, 0 = free
+    std::vector<int> free_slots_;
+    uint32_t n_used_ = 0;                // slots [0, n_used_) are scanned by the kernel
+    std::deque<uint64_t> queue_;
+    std::deque<uint64_t> done_;          // completed, unreleased, in completion order
+    std::unordered_map<uint64_t, Request> reqs_;
+    uint64_t next_id_ = 1;
+
+    unsigned long long* d_rk_ = nullptr;
+    double* d_rr_ = nullptr;
+    double* d_ri_ = nullptr;
+    size_t rcap_ = 0;
+
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    uint64_t steps_ = 0, launches_ = 0, upd_done_ = 0;
+    double busy_ms_ = 0.0;
+};
+
+}  // namespace sqc

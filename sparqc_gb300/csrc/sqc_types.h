@@ -63,6 +63,7 @@ struct Ctl {
     unsigned long long acc_nnz, acc_upd, acc_empty;
     unsigned long long amp_updates; // sum over gates of input nonzeros, since the last reset
     unsigned long long alg_bytes;   // algorithmic bytes of the passes, since the last reset
+    unsigned long long alg_bytes_pair;  // the part of alg_bytes moved by pair passes
     unsigned long long out_count;   // readout counter
     double acc[6];                  // reductions: norm, compare
     unsigned long long acc_max;     // bit pattern of a non-negative double (max |a-b|)

@@ -21,7 +21,15 @@ FP64, FP32 = 64, 32
 EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_state", "sqc_set_state",
            "sqc_apply_gates", "sqc_x", "sqc_y", "sqc_z", "sqc_h", "sqc_phase", "sqc_rz", "sqc_rx", "sqc_ry",
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
-           "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed")
+           "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
+           "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
+           "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
+           "sqc_batch_autotune", "sqc_batch_get_stats", "sqc_batch_compare", "sqc_batch_last_error",
+           "sqc_batch_stream",
+           "sqc_server_default_options", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
+           "sqc_server_step", "sqc_server_completed", "sqc_server_request_status", "sqc_server_nnz",
+           "sqc_server_get_state", "sqc_server_release", "sqc_server_get_stats", "sqc_server_compare",
+           "sqc_server_last_error", "sqc_server_stream")
 
 
 class HashTableParameters(ctypes.Structure):
@@ -33,12 +41,55 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_uint32), ("prune_threshold", ctypes.c_double),
                 ("load_factor", ctypes.c_double), ("initial_buckets", ctypes.c_uint64),
                 ("stream", ctypes.c_void_p), ("device", ctypes.c_uint32),
-                ("max_fused_gates", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+                ("max_fused_gates", ctypes.c_uint32), ("time_passes", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("gates_applied", "passes", "kernel_launches", "buckets",
-                                                "table_bytes", "replays", "amp_updates", "alg_bytes")]
+                                                "table_bytes", "replays", "amp_updates", "alg_bytes",
+                                                "alg_bytes_pair", "passes_pair", "pass_ns_pair", "pass_ns_stream")]
+
+
+class CircuitDesc(ctypes.Structure):
+    _fields_ = [("nq", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("gates", ctypes.c_void_p),
+                ("n_gates", ctypes.c_uint64)]
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_uint32), ("device", ctypes.c_uint32), ("stream", ctypes.c_void_p),
+                ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
+                ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("memory_budget", ctypes.c_uint64), ("use_graph", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 5)]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("load_factor", ctypes.c_double), ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double), ("candidates", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("circuits", ctypes.c_uint64), ("passes", ctypes.c_uint64), ("amp_updates", ctypes.c_uint64),
+                ("alg_bytes", ctypes.c_uint64), ("table_bytes", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64), ("last_run_ms", ctypes.c_double)]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_uint32), ("device", ctypes.c_uint32), ("stream", ctypes.c_void_p),
+                ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
+                ("memory_budget", ctypes.c_uint64), ("max_slots", ctypes.c_uint32), ("min_chunk", ctypes.c_uint32),
+                ("slice_ms", ctypes.c_double), ("reserved", ctypes.c_uint32 * 6)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_uint64), ("running", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("steps", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("amp_updates", ctypes.c_uint64),
+                ("pool_bytes", ctypes.c_uint64), ("pool_used", ctypes.c_uint64), ("busy_ms", ctypes.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE = 0, 1, 2
 
 
 class SparqcError(RuntimeError):
@@ -83,6 +134,47 @@ def load(path=LIB_PATH):
     L.sqc_last_error.restype = ctypes.c_char_p
     L.sqc_stream.argtypes = [P]
     L.sqc_stream.restype = P
+    L.sqc_batch_default_options.argtypes = [ctypes.POINTER(BatchOptions)]
+    L.sqc_batch_default_options.restype = None
+    L.sqc_batch_create.argtypes = [ctypes.POINTER(BatchOptions), ctypes.POINTER(P)]
+    L.sqc_batch_destroy.argtypes = [P]
+    L.sqc_batch_prepare.argtypes = [P, P, U32]
+    L.sqc_batch_run.argtypes = [P]
+    L.sqc_batch_sync.argtypes = [P]
+    L.sqc_batch_circuit_status.argtypes = [P, U32, ctypes.POINTER(I)]
+    L.sqc_batch_nnz.argtypes = [P, U32, ctypes.POINTER(U64)]
+    L.sqc_batch_get_state.argtypes = [P, U32, P, P, P, U64, ctypes.POINTER(U64), U32]
+    L.sqc_batch_autotune.argtypes = [P, ctypes.POINTER(BatchTuning)]
+    L.sqc_batch_get_stats.argtypes = [P, ctypes.POINTER(BatchStats)]
+    L.sqc_batch_last_error.argtypes = [P]
+    L.sqc_batch_last_error.restype = ctypes.c_char_p
+    L.sqc_batch_stream.argtypes = [P]
+    L.sqc_batch_stream.restype = P
+    L.sqc_server_default_options.argtypes = [ctypes.POINTER(ServerOptions)]
+    L.sqc_server_default_options.restype = None
+    L.sqc_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(P)]
+    L.sqc_server_destroy.argtypes = [P]
+    L.sqc_server_submit.argtypes = [P, ctypes.POINTER(CircuitDesc), ctypes.POINTER(U64)]
+    L.sqc_server_step.argtypes = [P, ctypes.POINTER(U32)]
+    L.sqc_server_completed.argtypes = [P, P, U32, ctypes.POINTER(U32)]
+    L.sqc_server_request_status.argtypes = [P, U64, ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.sqc_server_nnz.argtypes = [P, U64, ctypes.POINTER(U64)]
+    L.sqc_server_get_state.argtypes = [P, U64, P, P, P, U64, ctypes.POINTER(U64), U32]
+    L.sqc_server_release.argtypes = [P, U64]
+    L.sqc_server_get_stats.argtypes = [P, ctypes.POINTER(ServerStats)]
+    L.sqc_batch_compare.argtypes = [P, U32, P, ctypes.POINTER(D), ctypes.POINTER(D)]
+    L.sqc_server_compare.argtypes = [P, U64, P, ctypes.POINTER(D), ctypes.POINTER(D)]
+    L.sqc_server_last_error.argtypes = [P]
+    L.sqc_server_last_error.restype = ctypes.c_char_p
+    L.sqc_server_stream.argtypes = [P]
+    L.sqc_server_stream.restype = P
+    for n in ("sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare", "sqc_batch_run", "sqc_batch_sync",
+              "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state", "sqc_batch_autotune",
+              "sqc_batch_get_stats", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
+              "sqc_server_step", "sqc_server_completed", "sqc_server_request_status", "sqc_server_nnz",
+              "sqc_server_get_state", "sqc_server_release", "sqc_server_get_stats", "sqc_batch_compare",
+              "sqc_server_compare"):
+        getattr(L, n).restype = I
     for n in EXPORTS:
         f = getattr(L, n)
         if f.restype is ctypes.c_int or n in ("sqc_create", "sqc_destroy", "sqc_set_zero_state", "sqc_set_state",
@@ -102,7 +194,7 @@ class State:
     """A sparse statevector of ``nq`` qubits on one GPU, starting in |0...0>."""
 
     def __init__(self, nq, precision=FP64, prune_threshold=1e-14, load_factor=0.5, initial_buckets=0,
-                 stream=None, device=0, max_fused_gates=0, params=None):
+                 stream=None, device=0, max_fused_gates=0, params=None, time_passes=False):
         self._L = load()
         o = Options()
         self._L.sqc_default_options(ctypes.byref(o))
@@ -113,6 +205,7 @@ class State:
         o.stream = stream
         o.device = device
         o.max_fused_gates = max_fused_gates
+        o.time_passes = 1 if time_passes else 0
         h = ctypes.c_void_p()
         pp = ctypes.byref(params) if params is not None else None
         rc = self._L.sqc_create(nq, pp, ctypes.byref(o), ctypes.byref(h))
@@ -240,3 +333,226 @@ class Circuit(State):
         k, r, i = self.state(sorted=True, drop_negligible=True)
         for kk, rr, ii in zip(k, r, i):
             print(f"{int(kk)}: \t{rr: .3e} + {ii: .3e}j")
+
+
+class Batch:
+    """Many independent circuits, each from |0...0>, run by one persistent kernel launch.
+
+    ``circuits`` is a list of ``(nq, gates)`` with ``gates`` a GATE_DTYPE array. Each
+    circuit's result is bit-identical to running it alone on a ``State``.
+    """
+
+    def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, min_chunk=8, blocks_per_sm=0,
+                 memory_budget=0, use_graph=False, stream=None, device=0):
+        self._L = load()
+        o = BatchOptions()
+        self._L.sqc_batch_default_options(ctypes.byref(o))
+        o.precision = precision
+        o.prune_threshold = prune_threshold
+        o.load_factor = load_factor
+        o.min_chunk = min_chunk
+        o.blocks_per_sm = blocks_per_sm
+        o.memory_budget = memory_budget
+        o.use_graph = 1 if use_graph else 0
+        o.stream = stream
+        o.device = device
+        h = ctypes.c_void_p()
+        rc = self._L.sqc_batch_create(ctypes.byref(o), ctypes.byref(h))
+        if rc != OK:
+            raise SparqcError(rc, f"sqc_batch_create: {self._L.sqc_status_string(rc).decode()}")
+        self._h = h
+        self.precision = precision
+        self._keep = []
+        self.n = 0
+
+    def _check(self, rc, what):
+        if rc != OK:
+            msg = self._L.sqc_batch_last_error(self._h).decode() if self._h else ""
+            raise SparqcError(rc, f"{what}: {self._L.sqc_status_string(rc).decode()} ({msg})")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sqc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return self._L.sqc_batch_stream(self._h)
+
+    def prepare(self, circuits):
+        descs = (CircuitDesc * max(len(circuits), 1))()
+        keep = []
+        for i, (nq, gates) in enumerate(circuits):
+            g = np.ascontiguousarray(gates, GATE_DTYPE)
+            keep.append(g)
+            descs[i].nq = nq
+            descs[i].gates = g.ctypes.data
+            descs[i].n_gates = g.size
+        self._check(self._L.sqc_batch_prepare(self._h, descs, len(circuits)), "batch prepare")
+        self.n = len(circuits)
+
+    def run(self):
+        self._check(self._L.sqc_batch_run(self._h), "batch run")
+
+    def sync(self):
+        self._check(self._L.sqc_batch_sync(self._h), "batch sync")
+
+    def status(self, i):
+        s = ctypes.c_int()
+        self._check(self._L.sqc_batch_circuit_status(self._h, i, ctypes.byref(s)), "batch status")
+        return s.value
+
+    def nnz(self, i):
+        n = ctypes.c_uint64()
+        self._check(self._L.sqc_batch_nnz(self._h, i, ctypes.byref(n)), "batch nnz")
+        return n.value
+
+    def state(self, i, sorted=True, drop_negligible=False):
+        n = self.nnz(i)
+        keys = np.empty(max(n, 1), np.uint64)
+        re = np.empty(max(n, 1), np.float64)
+        im = np.empty(max(n, 1), np.float64)
+        got = ctypes.c_uint64()
+        flags = (READ_SORTED if sorted else 0) | (READ_DROP_NEGLIGIBLE if drop_negligible else 0)
+        self._check(self._L.sqc_batch_get_state(self._h, i, _p(keys), _p(re), _p(im), n, ctypes.byref(got), flags),
+                    "batch get_state")
+        m = got.value
+        return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def compare(self, i, ref):
+        """(fidelity, max abs error) of circuit i against a State of the same qubit count."""
+        f, e = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.sqc_batch_compare(self._h, i, ref.handle, ctypes.byref(f), ctypes.byref(e)),
+                    "batch compare")
+        return f.value, e.value
+
+    def autotune(self):
+        t = BatchTuning()
+        self._check(self._L.sqc_batch_autotune(self._h, ctypes.byref(t)), "batch autotune")
+        return {n: getattr(t, n) for n, _ in BatchTuning._fields_ if n != "reserved"}
+
+    def stats(self):
+        s = BatchStats()
+        self._check(self._L.sqc_batch_get_stats(self._h, ctypes.byref(s)), "batch stats")
+        return {n: getattr(s, n) for n, _ in BatchStats._fields_}
+
+
+class Server:
+    """Serving loop: circuits submitted one by one share the GPU with those already running.
+
+    ``submit(nq, gates)`` queues a circuit and returns its request id; every ``step()`` admits
+    what fits the memory budget and runs one time slice of all resident circuits; completed
+    requests are listed by ``completed()`` and read with ``state(id)`` until ``release(id)``.
+    """
+
+    def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, memory_budget=0, max_slots=1024,
+                 min_chunk=8, slice_ms=2.0, stream=None, device=0):
+        self._L = load()
+        o = ServerOptions()
+        self._L.sqc_server_default_options(ctypes.byref(o))
+        o.precision = precision
+        o.prune_threshold = prune_threshold
+        o.load_factor = load_factor
+        o.memory_budget = memory_budget
+        o.max_slots = max_slots
+        o.min_chunk = min_chunk
+        o.slice_ms = slice_ms
+        o.stream = stream
+        o.device = device
+        h = ctypes.c_void_p()
+        rc = self._L.sqc_server_create(ctypes.byref(o), ctypes.byref(h))
+        if rc != OK:
+            raise SparqcError(rc, f"sqc_server_create: {self._L.sqc_status_string(rc).decode()}")
+        self._h = h
+        self.precision = precision
+
+    def _check(self, rc, what):
+        if rc != OK:
+            msg = self._L.sqc_server_last_error(self._h).decode() if self._h else ""
+            raise SparqcError(rc, f"{what}: {self._L.sqc_status_string(rc).decode()} ({msg})")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sqc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return self._L.sqc_server_stream(self._h)
+
+    def submit(self, nq, gates):
+        g = np.ascontiguousarray(gates, GATE_DTYPE)
+        d = CircuitDesc()
+        d.nq = nq
+        d.gates = g.ctypes.data
+        d.n_gates = g.size
+        rid = ctypes.c_uint64()
+        self._check(self._L.sqc_server_submit(self._h, ctypes.byref(d), ctypes.byref(rid)), "server submit")
+        return rid.value
+
+    def step(self):
+        n = ctypes.c_uint32()
+        self._check(self._L.sqc_server_step(self._h, ctypes.byref(n)), "server step")
+        return n.value
+
+    def completed(self, cap=1 << 16):
+        ids = np.empty(cap, np.uint64)
+        n = ctypes.c_uint32()
+        self._check(self._L.sqc_server_completed(self._h, _p(ids), cap, ctypes.byref(n)), "server completed")
+        return [int(x) for x in ids[:n.value]]
+
+    def status(self, rid):
+        st, code = ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.sqc_server_request_status(self._h, rid, ctypes.byref(st), ctypes.byref(code)),
+                    "server status")
+        return st.value, code.value
+
+    def nnz(self, rid):
+        n = ctypes.c_uint64()
+        self._check(self._L.sqc_server_nnz(self._h, rid, ctypes.byref(n)), "server nnz")
+        return n.value
+
+    def state(self, rid, sorted=True, drop_negligible=False):
+        n = self.nnz(rid)
+        keys = np.empty(max(n, 1), np.uint64)
+        re = np.empty(max(n, 1), np.float64)
+        im = np.empty(max(n, 1), np.float64)
+        got = ctypes.c_uint64()
+        flags = (READ_SORTED if sorted else 0) | (READ_DROP_NEGLIGIBLE if drop_negligible else 0)
+        self._check(self._L.sqc_server_get_state(self._h, rid, _p(keys), _p(re), _p(im), n, ctypes.byref(got),
+                                                 flags), "server get_state")
+        m = got.value
+        return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def compare(self, rid, ref):
+        """(fidelity, max abs error) of a completed request against a State of the same qubit count."""
+        f, e = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.sqc_server_compare(self._h, rid, ref.handle, ctypes.byref(f), ctypes.byref(e)),
+                    "server compare")
+        return f.value, e.value
+
+    def release(self, rid):
+        self._check(self._L.sqc_server_release(self._h, rid), "server release")
+
+    def stats(self):
+        s = ServerStats()
+        self._check(self._L.sqc_server_get_stats(self._h, ctypes.byref(s)), "server stats")
+        return {n: getattr(s, n) for n, _ in ServerStats._fields_}

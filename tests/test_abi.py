@@ -51,8 +51,10 @@ def test_struct_layouts_match(tmp_path, lib_path):
 #include <stddef.h>
 #include "sparqc.h"
 int main(void) {
-    printf("%zu %zu %zu %zu %zu %zu\n", sizeof(sqc_gate), offsetof(sqc_gate, controls),
-           offsetof(sqc_gate, lambda), sizeof(sqc_options), sizeof(sqc_hash_table_parameters), sizeof(sqc_stats));
+    printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sqc_gate), offsetof(sqc_gate, controls),
+           offsetof(sqc_gate, lambda), sizeof(sqc_options), sizeof(sqc_hash_table_parameters), sizeof(sqc_stats),
+           sizeof(sqc_circuit_desc), sizeof(sqc_batch_options), sizeof(sqc_batch_tuning), sizeof(sqc_batch_stats),
+           offsetof(sqc_options, time_passes), sizeof(sqc_server_options), sizeof(sqc_server_stats));
     return 0;
 }
 ''')
@@ -65,6 +67,13 @@ int main(void) {
     assert vals[3] == ctypes.sizeof(engine.Options)
     assert vals[4] == ctypes.sizeof(engine.HashTableParameters)
     assert vals[5] == ctypes.sizeof(engine.Stats)
+    assert vals[6] == ctypes.sizeof(engine.CircuitDesc)
+    assert vals[7] == ctypes.sizeof(engine.BatchOptions)
+    assert vals[8] == ctypes.sizeof(engine.BatchTuning)
+    assert vals[9] == ctypes.sizeof(engine.BatchStats)
+    assert vals[10] == engine.Options.time_passes.offset
+    assert vals[11] == ctypes.sizeof(engine.ServerOptions)
+    assert vals[12] == ctypes.sizeof(engine.ServerStats)
 
 
 def test_cpp_dropin_header_compiles(tmp_path):
