@@ -53,7 +53,8 @@ unsigned long long slice_buckets(unsigned long long bound, double lf) {
     return std::max(kMinSliceBuckets, pow2_at_least((unsigned long long)want));
 }
 
-const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_run, CircuitPlan* out) {
+const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_run, uint32_t max_nx,
+                         CircuitPlan* out) {
     if (nq < 1 || nq > 64) return "qubit count must be 1..64";
     if (n && !gates) return "null gate array";
     CircuitPlan& c = *out;
@@ -73,9 +74,18 @@ const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_
         c.desc.push_back(d);
     }
     c.end = p;
-    split_passes(c.desc.data(), c.desc.size(), max_run, [&](size_t g0, size_t g1, bool pair, bool fixed) {
-        c.passes.push_back(BPass{(uint32_t)g0, (uint32_t)g1, pair ? 1u : 0u, fixed ? 1u : 0u});
-    });
+    split_passes(c.desc.data(), c.desc.size(), max_run, max_nx,
+                 [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, bool fixed) {
+                     BPass b;
+                     std::memset(&b, 0, sizeof b);
+                     b.g0 = (uint32_t)g0;
+                     b.g1 = (uint32_t)g1;
+                     b.nx = (uint16_t)nx;
+                     b.keys_fixed = fixed ? 1 : 0;
+                     b.q1 = (uint8_t)(nx >= 1 ? q1 : 0xFF);
+                     b.q2 = (uint8_t)(nx >= 2 ? q2 : 0xFF);
+                     c.passes.push_back(b);
+                 });
     if (c.passes.size() > kMaxBatchPasses) return "too many passes for a batch circuit";
     c.bound = group_bound(p, nq);
     return nullptr;
@@ -157,7 +167,7 @@ int Batch::prepare(const sqc_circuit_desc* cs, uint32_t n) {
     if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
     std::vector<CircuitPlan> plans(n);
     for (uint32_t i = 0; i < n; ++i) {
-        if (const char* why = plan_circuit(cs[i].nq, cs[i].gates, cs[i].n_gates, kMaxRun, &plans[i]))
+        if (const char* why = plan_circuit(cs[i].nq, cs[i].gates, cs[i].n_gates, kMaxRun, 2, &plans[i]))
             return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": " + why);
     }
     plans_.swap(plans);
@@ -261,6 +271,7 @@ int Batch::layout() {
         c.passes = d_pass_ + poff;
         c.npasses = (uint32_t)plans_[i].passes.size();
         c.max_groups = (unsigned long long)(0.9 * (double)nb);
+        c.bound = plans_[i].bound;
         doff += plans_[i].desc.size();
         poff += plans_[i].passes.size();
     }

@@ -66,56 +66,29 @@ __device__ __forceinline__ void stream_chunk(const TableDev& t, const GateDesc* 
         const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
         load_val_g<T>(t, va, Ga, ba, j);
         load_val_g<T>(t, vb, Gb, bb, j);
-        run_gates<T>(gates, g0, g1, false, va, vb, lane, pb, upd);
+        run_gates<T>(gates, g0, g1, kNoQubit, kNoQubit, va, vb, lane, pb, upd);
         write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
     }
 }
 
-// Pair pass over list entries [eb, ee): lanes 0..3 settle the ownership of four entries,
-// the owned pairs are processed two per warp step (one per half).
-template <class T>
-__device__ __forceinline__ void pair_chunk(const TableDev& t, const GateDesc* gates, uint32_t g0, uint32_t g1,
-                                           unsigned ep, Ctl* ctl, unsigned long long eb, unsigned long long ee,
-                                           const PruneBits& pb, unsigned long long& cnt_nnz,
+// Pass that pairs groups over list entries [eb, ee), four entries at a time (units4 and
+// run_units4 of sqc_pass_dev.cuh).
+template <class T, int NX>
+__device__ __forceinline__ void unit_chunk(const TableDev& t, const GateDesc* gates, uint32_t g0, uint32_t g1,
+                                           uint32_t q1, uint32_t q2, unsigned ep, Ctl* ctl, unsigned long long eb,
+                                           unsigned long long ee, const PruneBits& pb, unsigned long long& cnt_nnz,
                                            unsigned long long& cnt_empty, unsigned long long& upd) {
-    const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
-    const uint32_t q = __ldg(&gates[g0].target);
-    const unsigned long long m = 1ULL << (q - kSlotBits);
+    const int lane = threadIdx.x & 31;
+    const unsigned long long m1 = 1ULL << (q1 - kSlotBits);
+    const unsigned long long m2 = NX == 2 ? 1ULL << (q2 - kSlotBits) : 0ULL;
     Val<T> va, vb;
     for (unsigned long long e0 = eb; e0 < ee; e0 += 4) {
-        bool owner = false;
-        long long b0 = -1, b1 = -1;
-        unsigned long long G0 = 0;
-        if (lane < 4 && e0 + lane < ee) {
-            const long long b = (long long)t.list[e0 + lane];
-            const unsigned long long G = load_hdr(t.hdr + b).group;
-            const bool mine1 = (G & m) != 0;
-            const long long bp = lookup_group(t, ep, G ^ m);
-            owner = !mine1 || bp < 0;
-            b0 = mine1 ? bp : b;
-            b1 = mine1 ? b : bp;
-            G0 = G & ~m;
-        }
-        unsigned om = __ballot_sync(kFull, owner) & 0xFu;
-        while (om) {
-            const int u0 = __ffs(om) - 1;
-            om &= om - 1;
-            int u1 = -1;
-            if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
-            const int u = half ? u1 : u0;
-            const int src = u >= 0 ? u : u0;
-            const long long ub0 = (long long)shfl64((unsigned long long)b0, src);
-            const long long ub1 = (long long)shfl64((unsigned long long)b1, src);
-            const unsigned long long uG0 = shfl64(G0, src);
-            const bool act = u >= 0;
-            load_val_g<T>(t, va, uG0, act ? ub0 : -1, j);
-            load_val_g<T>(t, vb, uG0 | m, act ? ub1 : -1, j);
-            run_gates<T>(gates, g0, g1, true, va, vb, lane, pb, upd);
-            const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
-            const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
-            append_new(t, ctl, fa, fb, lane);
-        }
+        long long mb;
+        unsigned long long G0;
+        const unsigned om = units4<NX>(t, ep, e0, ee, m1, m2, lane, &mb, &G0);
+        run_units4<T, NX>(t, ep, ctl, gates, g0, g1, q1, q2, m1, m2, om, mb, G0, lane, pb, va, vb, cnt_nnz, cnt_empty,
+                          upd);
     }
 }
 
@@ -139,7 +112,7 @@ __device__ void finish_circuit_pass(const BatchArgs& a, unsigned c, const BCirc&
         const unsigned long long A = a.amp_bytes;
         const unsigned long long ab = bp.keys_fixed ? nnz_in * (8ULL + 2ULL * A) : (nnz_in + tn) * (8ULL + A);
         ctl->alg_bytes += ab;
-        if (bp.pair) ctl->alg_bytes_pair += ab;
+        if (bp.nx) ctl->alg_bytes_pair += ab;
         ctl->seq += 1;
     }
     const unsigned next = p + 1;
@@ -151,8 +124,9 @@ __device__ void finish_circuit_pass(const BatchArgs& a, unsigned c, const BCirc&
         state = BS_DONE;
     } else {
         const unsigned long long n = ctl->list_n;
-        const BPass nx = C.passes[next];
-        if (nx.pair && 2 * n > C.max_groups) {   // the slice could overflow: stop before touching it
+        const BPass nxp = C.passes[next];
+        const unsigned long long grown = umin64(C.bound, n << nxp.nx);
+        if (nxp.nx && grown > C.max_groups) {   // the slice could overflow: stop before touching it
             atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
             state = BS_FAILED;
         } else {
@@ -240,8 +214,14 @@ __global__ void __launch_bounds__(kBatchThreads, MINB) batch_run_kernel(BatchArg
         unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
         const unsigned cst = __shfl_sync(kFull, *(volatile unsigned int*)&ctl->status, 0);
         if (eb < ee && cst == 0) {
-            if (bp.pair) pair_chunk<T>(C.t, C.gates, bp.g0, bp.g1, ep, ctl, eb, ee, a.prune, cnt_nnz, cnt_empty, upd);
-            else stream_chunk<T>(C.t, C.gates, bp.g0, bp.g1, ep, ctl, eb, ee, a.prune, cnt_nnz, cnt_empty, upd);
+            if (bp.nx == 1)
+                unit_chunk<T, 1>(C.t, C.gates, bp.g0, bp.g1, bp.q1, kNoQubit, ep, ctl, eb, ee, a.prune, cnt_nnz,
+                                 cnt_empty, upd);
+            else if (bp.nx == 2)
+                unit_chunk<T, 2>(C.t, C.gates, bp.g0, bp.g1, bp.q1, bp.q2, ep, ctl, eb, ee, a.prune, cnt_nnz,
+                                 cnt_empty, upd);
+            else
+                stream_chunk<T>(C.t, C.gates, bp.g0, bp.g1, ep, ctl, eb, ee, a.prune, cnt_nnz, cnt_empty, upd);
         }
         cnt_nnz = warp_sum(cnt_nnz);
         cnt_empty = warp_sum(cnt_empty);

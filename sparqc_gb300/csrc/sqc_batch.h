@@ -43,7 +43,8 @@ struct CircuitPlan {
 };
 
 // Plan a circuit from |0...0>. Returns nullptr or the reason it cannot be batched.
-const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_run, CircuitPlan* out);
+const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_run, uint32_t max_nx,
+                         CircuitPlan* out);
 
 class Batch {
 public:

@@ -16,8 +16,10 @@ namespace sqc {
 // One pass of a circuit: gates [g0, g1) of its descriptors.
 struct BPass {
     uint32_t g0, g1;
-    uint32_t pair;        // the first gate pairs groups
-    uint32_t keys_fixed;  // diagonal gates only
+    uint16_t nx;          // cross-group qubits: 0, 1 or 2
+    uint16_t keys_fixed;  // diagonal gates only
+    uint8_t q1, q2;       // the cross-group qubits (>= 4; unused ones 0xFF)
+    uint8_t pad[2];
 };
 
 // A circuit of the batch (read-only while the kernel runs).
@@ -27,7 +29,8 @@ struct BCirc {
     const BPass* passes;
     uint32_t npasses;
     uint32_t pad;
-    unsigned long long max_groups;  // a pair pass refuses to start above max_groups / 2 buckets
+    unsigned long long max_groups;  // groups the slice takes (0.9 of its buckets)
+    unsigned long long bound;       // groups the circuit can ever hold (host-side bound)
 };
 
 // Scheduling word of a circuit: (pass << 44) | (chunks << 22) | chunks issued. A warp takes a

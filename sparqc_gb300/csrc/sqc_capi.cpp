@@ -48,7 +48,8 @@ void sqc_default_options(sqc_options* opt) {
     opt->device = 0;
     opt->max_fused_gates = 0;
     opt->time_passes = 0;
-    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
+    opt->max_cross_qubits = 0;
+    for (int i = 0; i < 2; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt, sqc_state** out) {

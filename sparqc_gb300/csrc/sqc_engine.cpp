@@ -78,6 +78,8 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     thr_ = o.prune_threshold;
     lf_ = o.load_factor;
     max_run_ = o.max_fused_gates ? std::min<uint32_t>(o.max_fused_gates, kMaxRun) : kMaxRun;
+    if (o.max_cross_qubits > 2) return fail(SQC_ERR_ARG, "max_cross_qubits must be 0, 1 or 2");
+    max_nx_ = o.max_cross_qubits ? o.max_cross_qubits : 2;
     time_passes_ = o.time_passes != 0;
     device_ = (int)o.device;
 
@@ -314,22 +316,30 @@ int Engine::flush() {
     a.prune = prune_;
     cudaEvent_t ev_prev = nullptr;
     if (time_passes_ && (rc = record_event(&ev_prev))) return rc;
-    size_t i = 0;
-    while (i < nd) {
-        const size_t start = i;
-        const bool pair = !streamable(hd[i]);
-        if (pair) ++i;
-        while (i < nd && i - start < max_run_ && streamable(hd[i])) ++i;
-        bool fixed = true;
-        for (size_t k = start; k < i; ++k) fixed = fixed && is_diag_kind(hd[k].kind);
-        a.g0 = (uint32_t)start;
-        a.g1 = (uint32_t)i;
-        a.pair = pair ? 1u : 0u;
-        a.keys_fixed = fixed ? 1u : 0u;
-        if (pair) list_hint_ = std::min<unsigned long long>(tab_.nb, 2 * list_hint_);
+    struct Span {
+        size_t g0, g1;
+        uint32_t nx, q1, q2;
+        bool fixed;
+    };
+    std::vector<Span> spans;
+    split_passes(hd, nd, max_run_, max_nx_, [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, bool fixed) {
+        spans.push_back(Span{g0, g1, nx, q1, q2, fixed});
+    });
+    for (const Span& sp : spans) {
+        const size_t i = sp.g1;
+        a.g0 = (uint32_t)sp.g0;
+        a.g1 = (uint32_t)sp.g1;
+        a.nx = sp.nx;
+        a.q1 = sp.q1;
+        a.q2 = sp.q2;
+        a.keys_fixed = sp.fixed ? 1u : 0u;
+        a.grow_bound = group_bound(after[i - 1], nq_);
+        if (sp.nx)
+            list_hint_ = std::min<unsigned long long>(tab_.nb, std::min(list_hint_ << sp.nx, a.grow_bound));
         a.range = pass_range(list_hint_, sms_);
         const int nl = launch_pass(a, list_hint_, dbl_, sms_, stream_);
         if (nl < 0) return cuda(cudaGetLastError(), "gate pass");
+        const bool pair = sp.nx > 0;
         if (time_passes_) {
             cudaEvent_t ev = nullptr;
             if ((rc = record_event(&ev))) return rc;

@@ -81,6 +81,7 @@ private:
     double thr_ = 1e-14;
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
+    uint32_t max_nx_ = 2;        // cross-group qubits per pass at most
     size_t budget_ = 0;
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;

@@ -180,7 +180,10 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
         for (size_t k = start; k < i; ++k) fixed = fixed && diag_kind(hd[k].kind);
         a.g0 = (uint32_t)start;
         a.g1 = (uint32_t)i;
-        a.pair = pair ? 1u : 0u;
+        a.nx = pair ? 1u : 0u;
+        a.q1 = pair ? hd[start].target : kNoQubit;
+        a.q2 = kNoQubit;
+        a.grow_bound = ~0ULL;
         a.keys_fixed = fixed ? 1u : 0u;
         if (launch_pass(a, kFixedBuckets, true, sms, st) < 0) return SQC_ERR_CUDA;
     }

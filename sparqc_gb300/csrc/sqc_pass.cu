@@ -78,12 +78,18 @@ __device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e
 // they save: each warp takes four list entries at a time, settles ownership inline (four
 // lookups in parallel), packs owned pairs two per warp and loads its slots straight into
 // registers.
-template <class T, bool PAIR>
+// True when a pass with nx cross-group qubits could leave more groups than the table takes.
+__device__ __forceinline__ bool could_overflow(const PassArgs& a, unsigned long long n) {
+    const unsigned long long grown = umin64(a.grow_bound, n << a.nx);
+    return grown > a.max_groups;
+}
+
+template <class T, int NX>
 __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
-    if (PAIR && 2 * n > a.max_groups) {   // could overflow: refuse before touching the state
+    if (NX > 0 && could_overflow(a, n)) {   // refuse before touching the state
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
         return;
     }
@@ -95,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
     Val<T> va, vb;
-    if (!PAIR) {
+    if (NX == 0) {
         for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
             const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
             const long long ba = ea < n ? (long long)t.list[ea] : -1;
@@ -104,67 +110,40 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
             const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
             load_val_g<T>(t, va, Ga, ba, j);
             load_val_g<T>(t, vb, Gb, bb, j);
-            run_gates<T>(a.gates, a.g0, a.g1, false, va, vb, lane, a.prune, upd);
+            run_gates<T>(a.gates, a.g0, a.g1, kNoQubit, kNoQubit, va, vb, lane, a.prune, upd);
             write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
             write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         }
     } else {
-        const uint32_t q = __ldg(&a.gates[a.g0].target);
-        const unsigned long long m = 1ULL << (q - kSlotBits);
+        const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
+        const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
         for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
-            // lanes 0..3: one list entry each -> ownership and the pair's buckets
-            bool owner = false;
-            long long b0 = -1, b1 = -1;
-            unsigned long long G0 = 0;
-            if (lane < 4 && e0 + lane < n) {
-                const long long b = (long long)t.list[e0 + lane];
-                const unsigned long long G = load_hdr(t.hdr + b).group;
-                const bool mine1 = (G & m) != 0;
-                const long long bp = lookup_group(t, ep, G ^ m);
-                owner = !mine1 || bp < 0;
-                b0 = mine1 ? bp : b;
-                b1 = mine1 ? b : bp;
-                G0 = G & ~m;
-            }
-            unsigned om = __ballot_sync(kFull, owner) & 0xFu;
-            while (om) {
-                const int u0 = __ffs(om) - 1;
-                om &= om - 1;
-                int u1 = -1;
-                if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
-                const int u = half ? u1 : u0;
-                const int src = u >= 0 ? u : u0;
-                const long long ub0 = (long long)shfl64((unsigned long long)b0, src);
-                const long long ub1 = (long long)shfl64((unsigned long long)b1, src);
-                const unsigned long long uG0 = shfl64(G0, src);
-                const bool act = u >= 0;
-                load_val_g<T>(t, va, uG0, act ? ub0 : -1, j);
-                load_val_g<T>(t, vb, uG0 | m, act ? ub1 : -1, j);
-                run_gates<T>(a.gates, a.g0, a.g1, true, va, vb, lane, a.prune, upd);
-                const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
-                const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
-                append_new(t, ctl, fa, fb, lane);
-            }
+            long long mb;
+            unsigned long long G0;
+            const unsigned om = units4<NX>(t, ep, e0, n, m1, m2, lane, &mb, &G0);
+            run_units4<T, NX>(t, ep, ctl, a.gates, a.g0, a.g1, a.q1, a.q2, m1, m2, om, mb, G0, lane, a.prune, va, vb,
+                              cnt_nnz, cnt_empty, upd);
         }
     }
-    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, PAIR, a.amp_bytes);
+    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
 }
 
-// ---- resolve: ownership of every group pair, before a pair pass ---------------------------
+// ---- resolve: ownership of every unit, before a pass that pairs groups -------------------
 // The list is cut into ranges of R entries (R a multiple of 32, a power of two). One warp per
-// range writes the range's owned pairs densely at units[r*R ...] (warp ballot, no atomics)
+// range writes the range's owned units densely at units[r*R ...] (warp ballot, no atomics)
 // and their number to counts[r].
+template <int NX>
 __global__ void __launch_bounds__(256) resolve_kernel(PassArgs a) {
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
-    if (2 * n > a.max_groups) {   // the pass could overflow the table: refuse before touching the state
+    if (could_overflow(a, n)) {   // refuse before touching the state
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
         return;
     }
     const unsigned ep = ctl->epoch;
-    const uint32_t q = __ldg(&a.gates[a.g0].target);
-    const unsigned long long m = 1ULL << (q - kSlotBits);
+    const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
+    const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
     const TableDev t = a.t;
     const unsigned long long R = a.range;
     const unsigned long long nranges = (n + R - 1) / R;
@@ -179,13 +158,10 @@ __global__ void __launch_bounds__(256) resolve_kernel(PassArgs a) {
             bool own = false;
             if (e < e1) {
                 const unsigned b = t.list[e];
-                const unsigned long long G = load_hdr(t.hdr + b).group;
-                const bool mine1 = (G & m) != 0;
-                const long long bp = lookup_group(t, ep, G ^ m);
-                own = !mine1 || bp < 0;
-                u.G0 = G & ~m;
-                u.b0 = mine1 ? kNoBucket : b;
-                u.b1 = mine1 ? b : (bp < 0 ? kNoBucket : (unsigned)bp);
+                long long bk[4];
+                own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, bk, &u.G0);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
             }
             const unsigned om = __ballot_sync(kFull, own);
             if (own) t.units[e0 + cnt + __popc(om & ((1u << lane) - 1u))] = u;
@@ -241,16 +217,17 @@ struct SlotSource {
     unsigned long long stride, end;
 };
 
-template <class T, bool PAIR>
+template <class T, int NX>
 __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotSource& src, unsigned long long n,
-                                           unsigned long long R, unsigned long long m, int lane) {
+                                           unsigned long long R, unsigned long long m1, unsigned long long m2,
+                                           int lane) {
     constexpr uint32_t kAmp = (uint32_t)(sizeof(typename AmpT<T>::V) * kSlots);
     constexpr int kKeyChunks = 128 / 16, kAmpChunks = (int)(kAmp / 16);
-    constexpr int kChunks = 4 * (kKeyChunks + kAmpChunks) + (PAIR ? 0 : 4);
+    constexpr int kChunks = 4 * (kKeyChunks + kAmpChunks) + (NX ? 0 : 4);
     unsigned bk = kNoBucket;
     unsigned long long Gk = 0;
     bool any = false;
-    if (!PAIR) {
+    if (NX == 0) {
         if (src.next < src.end) {
             const unsigned long long e = 4 * src.next + (unsigned long long)lane;
             if (lane < 4 && e < n) bk = t.list[e];
@@ -258,21 +235,30 @@ __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotS
             any = true;
         }
     } else {
-        while (src.next < src.end && src.u >= src.c) {   // move to the next range with pairs
+        while (src.next < src.end && src.u >= src.c) {   // move to the next range with units
             src.next += src.stride;
             src.u = 0;
             src.c = src.next < src.end ? t.counts[src.next] : 0;
         }
         if (src.next < src.end) {
             const unsigned long long base = src.next * R + src.u;
-            const bool second = src.u + 1 < src.c;
-            const int k = lane & 3;
-            if (lane < 4 && (k < 2 || second)) {
-                const Unit un = t.units[base + (k >> 1)];
-                bk = (k & 1) ? un.b1 : un.b0;
-                Gk = (k & 1) ? (un.G0 | m) : un.G0;
+            if (NX == 1) {   // two pairs: buckets (G0, G0|m1) of units u and u + 1
+                const bool second = src.u + 1 < src.c;
+                const int k = lane & 3;
+                if (lane < 4 && (k < 2 || second)) {
+                    const Unit un = t.units[base + (k >> 1)];
+                    bk = (k & 1) ? un.b[1] : un.b[0];
+                    Gk = (k & 1) ? (un.G0 | m1) : un.G0;
+                }
+                src.u += 2;
+            } else {         // one quad: bucket k is member (k & 1, k >> 1)
+                if (lane < 4) {
+                    const Unit un = t.units[base];
+                    bk = lane == 0 ? un.b[0] : lane == 1 ? un.b[1] : lane == 2 ? un.b[2] : un.b[3];
+                    Gk = un.G0 | ((lane & 1) ? m1 : 0ULL) | ((lane & 2) ? m2 : 0ULL);
+                }
+                src.u += 1;
             }
-            src.u += 2;
             any = true;
         }
     }
@@ -312,7 +298,7 @@ __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotS
     cp_async_commit();
 }
 
-template <class T, bool PAIR>
+template <class T, int NX>
 __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Slot<T>* ring = reinterpret_cast<Slot<T>*>(smem_raw) + (threadIdx.x >> 5) * kDepth;
@@ -327,12 +313,14 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
     const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     const unsigned long long R = a.range;
-    const unsigned long long m = PAIR ? 1ULL << (__ldg(&a.gates[a.g0].target) - kSlotBits) : 0ULL;
+    const unsigned long long m1 = NX ? 1ULL << (a.q1 - kSlotBits) : 0ULL;
+    const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    const uint32_t q1 = NX ? a.q1 : kNoQubit, q2 = NX == 2 ? a.q2 : kNoQubit;
     SlotSource src;
     src.next = gw;
     src.stride = nw;
     src.u = 0;
-    if (!PAIR) {
+    if (NX == 0) {
         src.end = (n + 3) / 4;
         src.c = 0;
     } else {
@@ -340,10 +328,10 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
         src.c = src.next < src.end ? t.counts[src.next] : 0;
     }
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
-    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, PAIR>(ring[d], t, src, n, R, m, lane);
+    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, R, m1, m2, lane);
     Val<T> va, vb;
     for (unsigned long long step = 0;; ++step) {
-        issue_slot<T, PAIR>(ring[(step + kDepth - 1) % kDepth], t, src, n, R, m, lane);
+        issue_slot<T, NX>(ring[(step + kDepth - 1) % kDepth], t, src, n, R, m1, m2, lane);
         cp_async_wait<kDepth - 1>();
         __syncwarp();
         const Slot<T>& sl = ring[step % kDepth];
@@ -351,7 +339,7 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
         const int ka = 2 * half, kb = ka + 1;
         const unsigned ba = sl.b[ka], bb = sl.b[kb];
         unsigned long long Ga, Gb;
-        if (PAIR) {
+        if (NX) {
             Ga = sl.G[ka];
             Gb = sl.G[kb];
         } else {
@@ -361,13 +349,13 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
         load_val_s<T>(va, Ga, ba, sl, ka, jj);
         load_val_s<T>(vb, Gb, bb, sl, kb, jj);
         __syncwarp();
-        run_gates<T>(a.gates, a.g0, a.g1, PAIR, va, vb, lane, a.prune, upd);
+        run_gates<T>(a.gates, a.g0, a.g1, q1, q2, va, vb, lane, a.prune, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
-        if (PAIR) append_new(t, ctl, fa, fb, lane);
+        if (NX) append_new(t, ctl, fa, fb, lane);
     }
     cp_async_wait<0>();   // nothing may still be landing in shared memory when the block exits
-    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, PAIR, a.amp_bytes);
+    finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
 }
 
 template <class T>
@@ -375,33 +363,50 @@ constexpr size_t staged_smem() {
     return (size_t)kWarpsPerBlock * kDepth * sizeof(Slot<T>);
 }
 
+template <class K>
+int occupancy(K kernel, int threads, size_t smem) {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem);
+    return n > 0 ? n : 1;
+}
+
 // Resident blocks per SM of each staged-kernel instantiation (queried once per process).
-int staged_residency(bool dbl, bool pair) {
-    static int cache[4] = {0, 0, 0, 0};
-    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
+int staged_residency(bool dbl, int nx) {
+    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int& c = cache[dbl ? 1 : 0][nx];
     if (!c) {
-        int n = 0;
-        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<double, true>, kStagedThreads, staged_smem<double>());
-        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<double, false>, kStagedThreads, staged_smem<double>());
-        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<float, true>, kStagedThreads, staged_smem<float>());
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, staged_kernel<float, false>, kStagedThreads, staged_smem<float>());
-        c = n > 0 ? n : 1;
+        if (dbl) c = nx == 0 ? occupancy(staged_kernel<double, 0>, kStagedThreads, staged_smem<double>())
+                   : nx == 1 ? occupancy(staged_kernel<double, 1>, kStagedThreads, staged_smem<double>())
+                             : occupancy(staged_kernel<double, 2>, kStagedThreads, staged_smem<double>());
+        else c = nx == 0 ? occupancy(staged_kernel<float, 0>, kStagedThreads, staged_smem<float>())
+                 : nx == 1 ? occupancy(staged_kernel<float, 1>, kStagedThreads, staged_smem<float>())
+                           : occupancy(staged_kernel<float, 2>, kStagedThreads, staged_smem<float>());
     }
     return c;
 }
 
-int direct_residency(bool dbl, bool pair) {
-    static int cache[4] = {0, 0, 0, 0};
-    int& c = cache[(dbl ? 2 : 0) + (pair ? 1 : 0)];
+int direct_residency(bool dbl, int nx) {
+    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int& c = cache[dbl ? 1 : 0][nx];
     if (!c) {
-        int n = 0;
-        if (dbl && pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<double, true>, kThreads, 0);
-        else if (dbl) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<double, false>, kThreads, 0);
-        else if (pair) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<float, true>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, direct_kernel<float, false>, kThreads, 0);
-        c = n > 0 ? n : 1;
+        if (dbl) c = nx == 0 ? occupancy(direct_kernel<double, 0>, kThreads, 0)
+                   : nx == 1 ? occupancy(direct_kernel<double, 1>, kThreads, 0)
+                             : occupancy(direct_kernel<double, 2>, kThreads, 0);
+        else c = nx == 0 ? occupancy(direct_kernel<float, 0>, kThreads, 0)
+                 : nx == 1 ? occupancy(direct_kernel<float, 1>, kThreads, 0)
+                           : occupancy(direct_kernel<float, 2>, kThreads, 0);
     }
     return c;
+}
+
+template <class T, int NX>
+void launch_direct(const PassArgs& a, int grid, cudaStream_t st) {
+    direct_kernel<T, NX><<<grid, kThreads, 0, st>>>(a);
+}
+
+template <class T, int NX>
+void launch_staged(const PassArgs& a, int grid, cudaStream_t st) {
+    staged_kernel<T, NX><<<grid, kStagedThreads, staged_smem<T>(), st>>>(a);
 }
 
 constexpr unsigned long long kDirectMaxBuckets = 1ULL << 20;
@@ -416,35 +421,43 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
     // list_hint bounds the live-bucket count; grids are sized from it (one resident wave at
     // most); the kernels read the exact count. Tables of up to kDirectMaxBuckets buckets
     // (states that have never needed more) take the direct pass.
+    const int nx = (int)a.nx;
+    if (nx < 0 || nx > 2) return -1;
     if (a.t.mask + 1 <= kDirectMaxBuckets) {
-        const unsigned long long wave = (unsigned long long)sms * direct_residency(dbl, a.pair != 0);
+        const unsigned long long wave = (unsigned long long)sms * direct_residency(dbl, nx);
         const unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
         const int grid = (int)std::max<unsigned long long>(1, std::min(g, wave));
         if (dbl) {
-            if (a.pair) direct_kernel<double, true><<<grid, kThreads, 0, st>>>(a);
-            else direct_kernel<double, false><<<grid, kThreads, 0, st>>>(a);
+            if (nx == 0) launch_direct<double, 0>(a, grid, st);
+            else if (nx == 1) launch_direct<double, 1>(a, grid, st);
+            else launch_direct<double, 2>(a, grid, st);
         } else {
-            if (a.pair) direct_kernel<float, true><<<grid, kThreads, 0, st>>>(a);
-            else direct_kernel<float, false><<<grid, kThreads, 0, st>>>(a);
+            if (nx == 0) launch_direct<float, 0>(a, grid, st);
+            else if (nx == 1) launch_direct<float, 1>(a, grid, st);
+            else launch_direct<float, 2>(a, grid, st);
         }
         return cudaGetLastError() == cudaSuccess ? 1 : -1;
     }
     int launched = 0;
-    if (a.pair) {
+    if (nx) {
         const unsigned long long nranges = list_hint / a.range + 1;
         const unsigned long long rg = std::min<unsigned long long>((nranges + 7) / 8, (unsigned long long)sms * 8);
-        resolve_kernel<<<(int)std::max<unsigned long long>(rg, 1), 256, 0, st>>>(a);
+        const int g = (int)std::max<unsigned long long>(rg, 1);
+        if (nx == 1) resolve_kernel<1><<<g, 256, 0, st>>>(a);
+        else resolve_kernel<2><<<g, 256, 0, st>>>(a);
         ++launched;
     }
-    const unsigned long long items = a.pair ? list_hint / 2 + 1 : (list_hint + 3) / 4;
-    const unsigned long long wave = (unsigned long long)sms * staged_residency(dbl, a.pair != 0);
+    const unsigned long long items = nx == 2 ? list_hint + 1 : nx == 1 ? list_hint / 2 + 1 : (list_hint + 3) / 4;
+    const unsigned long long wave = (unsigned long long)sms * staged_residency(dbl, nx);
     const int grid = (int)std::max<unsigned long long>(1, std::min(wave, (items + 3) / 4));
     if (dbl) {
-        if (a.pair) staged_kernel<double, true><<<grid, kStagedThreads, staged_smem<double>(), st>>>(a);
-        else staged_kernel<double, false><<<grid, kStagedThreads, staged_smem<double>(), st>>>(a);
+        if (nx == 0) launch_staged<double, 0>(a, grid, st);
+        else if (nx == 1) launch_staged<double, 1>(a, grid, st);
+        else launch_staged<double, 2>(a, grid, st);
     } else {
-        if (a.pair) staged_kernel<float, true><<<grid, kStagedThreads, staged_smem<float>(), st>>>(a);
-        else staged_kernel<float, false><<<grid, kStagedThreads, staged_smem<float>(), st>>>(a);
+        if (nx == 0) launch_staged<float, 0>(a, grid, st);
+        else if (nx == 1) launch_staged<float, 1>(a, grid, st);
+        else launch_staged<float, 2>(a, grid, st);
     }
     ++launched;
     return cudaGetLastError() == cudaSuccess ? launched : -1;

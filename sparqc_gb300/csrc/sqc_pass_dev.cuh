@@ -40,14 +40,17 @@ struct GateHead {
     unsigned long long ctrl, cval;
 };
 
+// The descriptor's first 32 bytes in two vector loads: {kind, target, ctrl}, {cval, flip, pad}.
 __device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
+    const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(g));
+    const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(g) + 1);
     GateHead h;
-    h.kind = __ldg(&g->kind);
-    h.target = __ldg(&g->target);
-    h.flip = __ldg(&g->flip);
-    h.credit = __ldg(&g->pad);
-    h.ctrl = __ldg(&g->ctrl);
-    h.cval = __ldg(&g->cval);
+    h.kind = v0.x;
+    h.target = v0.y;
+    h.ctrl = (unsigned long long)v0.z | ((unsigned long long)v0.w << 32);
+    h.cval = (unsigned long long)v1.x | ((unsigned long long)v1.y << 32);
+    h.flip = v1.z;
+    h.credit = v1.w;
     return h;
 }
 
@@ -127,27 +130,63 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
     }
 }
 
-// Apply gates [g0, g1) to the two held slots; in a pair pass the first gate pairs them.
-// Lane 0 accumulates the amp-update count: every gate is credited with the present slots
-// it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
+// Apply gates [g0, g1) to the two held slots. Branching and swap gates on the pass's first
+// cross-group qubit q1 pair a with b (lane-local); those on the second one, q2, pair each lane
+// with lane ^ 16 (the other half holds the groups with the q2 bit set); every other gate acts
+// within a group (warp shuffle for qubits 0..3, lane-local for diagonal gates). Stream passes pass q1 = q2 =
+// kNoQubit. Lane 0 accumulates the amp-update count: every gate is credited with the present
+// slots it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
 template <class T>
-__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1,
-                                          bool pair_first, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
+__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, uint32_t q1,
+                                          uint32_t q2, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
                                           unsigned long long& upd) {
     const int j = lane & 15;
+    // present slots in the warp: only a branching gate changes the count (swap gates permute
+    // presence among slots that satisfy the same controls, diagonal gates keep it)
+    unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+    bool recount = false;
     for (uint32_t gi = g0; gi < g1; ++gi) {
         const GateDesc* g = gates + gi;
         const GateHead h = gate_head(g);
-        const unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        recount = is_branch(h.kind);
         if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
-        if (gi == g0 && pair_first) {
+        const bool cross = is_branch(h.kind) || is_swap(h.kind);
+        if (cross && h.target == q1) {
             pair_step<T>(g, h, a, b, j, pb);
             continue;
         }
-        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : 0;
+        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : (cross && h.target == q2 ? 16 : 0);
         gate_step<T>(g, h, off, a, j, pb);
         gate_step<T>(g, h, off, b, j, pb);
     }
+}
+
+// Ownership of the unit of list entry group G (bucket b) in a pass with nx cross-group qubits
+// (masks m1, m2): the unit's members are G0 | i0*m1 | i1*m2 (G0 = G with those bits cleared);
+// the owner is the member with the smallest index i0 + 2*i1 among those live at the start of
+// the pass -- for a pair this is the reference's rule (the bit-0 key owns the pair unless it
+// is absent, emulator/device/device_table_FC.cuh:62-110) lifted to groups. Fills the members'
+// buckets (-1 when absent) and returns whether G owns its unit. Members a pass creates are
+// only ever created by the unit's owner, after its own check, so the lookups are consistent.
+template <int NX>
+__device__ __forceinline__ bool unit_owner(const TableDev& t, unsigned ep, unsigned long long G, long long b,
+                                           unsigned long long m1, unsigned long long m2, long long bk[4],
+                                           unsigned long long* G0) {
+    constexpr int K = NX == 2 ? 4 : 2;
+    const int idx = ((G & m1) ? 1 : 0) | ((NX == 2 && (G & m2)) ? 2 : 0);
+    *G0 = G & ~(m1 | (NX == 2 ? m2 : 0ULL));
+    bk[0] = bk[1] = bk[2] = bk[3] = -1;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {   // a live member of smaller index owns the unit
+        if (k < idx && lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL)) >= 0) return false;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (k == idx) bk[k] = b;
+        else if (k > idx) bk[k] = lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL));
+    }
+    return true;
 }
 
 // Write a held slot back in place. A group absent at the start of the pass gets a bucket
@@ -218,6 +257,80 @@ __device__ __forceinline__ void load_val_g(const TableDev& t, Val<T>& v, unsigne
         }
     }
     v.pres0 = v.pres;
+}
+
+// Ownership of the units of the (up to) four list entries [e0, e0 + 4) ∩ [0, n) in one round
+// of lookups: with K = 2^NX members per unit, lane l < 4K looks up member k = l % K of the
+// unit of entry l / K. Returns the owner mask (bit e: entry e owns its unit, by unit_owner's
+// rule); afterwards lane e*K + k holds member k's bucket (*mb, -1 when absent) and lane e*K
+// the unit's base group (*G0).
+template <int NX>
+__device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsigned long long e0, unsigned long long n,
+                                           unsigned long long m1, unsigned long long m2, int lane, long long* mb,
+                                           unsigned long long* G0) {
+    constexpr int K = NX == 2 ? 4 : 2;
+    const int e = lane / K, k = lane % K;
+    bool valid = false;
+    int idx = 0;
+    *mb = -1;
+    *G0 = 0;
+    if (lane < 4 * K && e0 + e < n) {
+        const long long b = (long long)t.list[e0 + e];
+        const unsigned long long G = load_hdr(t.hdr + b).group;
+        idx = ((G & m1) ? 1 : 0) | ((NX == 2 && (G & m2)) ? 2 : 0);
+        *G0 = G & ~(m1 | m2);
+        valid = true;
+        *mb = k == idx ? b : lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL));
+    }
+    const unsigned live = __ballot_sync(kFull, *mb >= 0);
+    const bool own = valid && k == 0 && ((live >> (e * K)) & ((1u << idx) - 1u)) == 0;
+    const unsigned om = __ballot_sync(kFull, own);
+    unsigned res = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) res |= ((om >> (i * K)) & 1u) << i;
+    return res;
+}
+
+// Process the owned units of a units4 round: pairs two per warp step (one per half), quads one
+// per warp step (the half selects the q2 bit); each unit's groups are loaded straight from the
+// table, the gates applied, and the slots written back.
+template <class T, int NX>
+__device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates, uint32_t g0,
+                                           uint32_t g1, uint32_t q1, uint32_t q2, unsigned long long m1,
+                                           unsigned long long m2, unsigned om, long long mb, unsigned long long G0,
+                                           int lane, const PruneBits& pb, Val<T>& va, Val<T>& vb,
+                                           unsigned long long& cnt_nnz, unsigned long long& cnt_empty,
+                                           unsigned long long& upd) {
+    constexpr int K = NX == 2 ? 4 : 2;
+    const int half = lane >> 4, j = lane & 15;
+    while (om) {
+        int u, src;
+        if (NX == 1) {
+            const int u0 = __ffs(om) - 1;
+            om &= om - 1;
+            int u1 = -1;
+            if (om) { u1 = __ffs(om) - 1; om &= om - 1; }
+            u = half ? u1 : u0;
+            src = u >= 0 ? u : u0;
+        } else {
+            u = __ffs(om) - 1;
+            om &= om - 1;
+            src = u;
+        }
+        const bool hi = NX == 2 && half;
+        // this half's two members: (0, 1), or (2, 3) for the upper half of a quad
+        const long long xa = (long long)shfl64((unsigned long long)mb, src * K + (hi ? 2 : 0));
+        const long long xb = (long long)shfl64((unsigned long long)mb, src * K + (hi ? 3 : 1));
+        const unsigned long long uG0 = shfl64(G0, src * K);
+        const unsigned long long Ga = uG0 | (hi ? m2 : 0ULL);
+        const bool act = u >= 0;
+        load_val_g<T>(t, va, Ga, act ? xa : -1, j);
+        load_val_g<T>(t, vb, Ga | m1, act ? xb : -1, j);
+        run_gates<T>(gates, g0, g1, q1, NX == 2 ? q2 : kNoQubit, va, vb, lane, pb, upd);
+        const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+        const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        append_new(t, ctl, fa, fb, lane);
+    }
 }
 
 }  // namespace

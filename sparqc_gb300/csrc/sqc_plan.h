@@ -44,19 +44,31 @@ GateDesc make_desc(const Planner& p, uint32_t kind, uint32_t target, unsigned lo
 // is counted in p.credit, to be credited to the next device gate.
 bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out);
 
-// Passes of a descriptor sequence: either a run of at most max_run streamable gates, or one
-// cross-group gate followed by such a run. f(g0, g1, pair, keys_fixed) is called per pass.
+// Passes of a descriptor sequence. A pass is a run of at most max_run consecutive gates whose
+// cross-group gates (gates that pair keys of different 16-key groups) target at most
+// max_nx distinct qubits; streamable gates may sit anywhere in it. Passes are cut greedily.
+// f(g0, g1, nx, q1, q2, keys_fixed) is called per pass, q1/q2 the cross-group qubits in order
+// of first use (kNoQubit when absent).
 template <class F>
-void split_passes(const GateDesc* d, size_t n, size_t max_run, F&& f) {
+void split_passes(const GateDesc* d, size_t n, size_t max_run, uint32_t max_nx, F&& f) {
     size_t i = 0;
     while (i < n) {
         const size_t start = i;
-        const bool pair = !streamable(d[i]);
-        if (pair) ++i;
-        while (i < n && i - start < max_run && streamable(d[i])) ++i;
+        uint32_t q[2] = {kNoQubit, kNoQubit};
+        uint32_t nx = 0;
+        while (i < n && i - start < max_run) {
+            if (!streamable(d[i])) {
+                const uint32_t t = d[i].target;
+                if (t != q[0] && t != q[1]) {
+                    if (nx >= max_nx) break;
+                    q[nx++] = t;
+                }
+            }
+            ++i;
+        }
         bool fixed = true;
         for (size_t k = start; k < i; ++k) fixed = fixed && is_diag_kind(d[k].kind);
-        f(start, i, pair, fixed);
+        f(start, i, nx, q[0], q[1], fixed);
     }
 }
 

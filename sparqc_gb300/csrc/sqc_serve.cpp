@@ -116,7 +116,7 @@ size_t Server::request_bytes(const Request& r) const {
 int Server::submit(const sqc_circuit_desc* c, uint64_t* id) {
     if (!c || !id) return fail(SQC_ERR_ARG, "null argument");
     Request r;
-    if (const char* why = plan_circuit(c->nq, c->gates, c->n_gates, kMaxRun, &r.plan)) return fail(SQC_ERR_ARG, why);
+    if (const char* why = plan_circuit(c->nq, c->gates, c->n_gates, kMaxRun, 2, &r.plan)) return fail(SQC_ERR_ARG, why);
     r.nb = slice_buckets(r.plan.bound, lf_);
     if (!r.nb || request_bytes(r) > alloc_.size())
         return fail(SQC_ERR_BUDGET, "the circuit's table slice can never fit the memory budget");
@@ -163,6 +163,7 @@ int Server::admit() {
         c.passes = dp;
         c.npasses = (uint32_t)r.plan.passes.size();
         c.max_groups = (unsigned long long)(0.9 * (double)r.nb);
+        c.bound = r.plan.bound;
         h_cmd_[slot] = BC_INIT;
         h_limit_[slot] = c.npasses;
         r.state = SQC_REQ_RUNNING;

@@ -29,13 +29,14 @@ struct alignas(16) Header {
     unsigned int aux;           // 0
 };
 
-// One group pair of a pair pass, resolved before the pass: G0 has the stored target bit 0;
-// b0/b1 are the buckets of G0 and G0 | m (kNoBucket when absent). Written per list entry;
-// entries whose group does not own its pair hold b0 = b1 = kNoBucket.
+// One unit of a pass that pairs groups, resolved before the pass. With cross-group qubits
+// q1 (mask m1 = 1 << (q1 - 4)) and, for a quad pass, q2 (m2), the unit is the set of groups
+// G0 | i0*m1 | i1*m2 with G0 having both stored bits 0; b[i0 + 2*i1] is the bucket of member
+// (i0, i1), kNoBucket when the group is absent. Pair passes use b[0], b[1].
 constexpr unsigned kNoBucket = 0xFFFFFFFFu;
 struct alignas(16) Unit {
     unsigned long long G0;
-    unsigned int b0, b1;
+    unsigned int b[4];
 };
 
 struct TableDev {
@@ -72,8 +73,9 @@ struct Ctl {
 // Gate descriptor with host-resolved coefficients (std::cos/std::sin on the host, so the
 // device and the CPU oracle use identical values) in the stored-key frame: the gate acts on
 // a stored key s iff (s & ctrl) == cval, and the member's logical target bit is
-// ((s >> target) & 1) ^ flip.
-struct GateDesc {
+// ((s >> target) & 1) ^ flip. The first 32 bytes (kind .. pad) are read as two 16-byte
+// vectors, hence the alignment.
+struct alignas(16) GateDesc {
     uint32_t kind, target;
     unsigned long long ctrl, cval;
     uint32_t flip, pad;
@@ -88,19 +90,24 @@ struct PruneBits {
     unsigned int f;         // bit pattern of the largest float below thr
 };
 
+constexpr uint32_t kNoQubit = 0xFFFFFFFFu;
+
 struct PassArgs {
     TableDev t;
     Ctl* ctl;
     const GateDesc* gates;
     uint32_t g0, g1;        // gate range [g0, g1) of this pass
-    uint32_t pair;          // 1: the first gate pairs groups G and G ^ (1 << (target - 4))
+    uint32_t nx;            // cross-group qubits of the pass: 0 (stream), 1 (pair) or 2 (quad)
     uint32_t keys_fixed;    // 1: every gate of the pass is diagonal (no key changes)
     uint32_t amp_bytes;     // 16 (FP64) or 8 (FP32)
     uint32_t credit;        // gates resolved on the host just before this pass (identity or
                             // relabel): each is credited with this pass's input key count
-    unsigned long long max_groups;   // a pair pass refuses to start above max_groups / 2 buckets
+    unsigned long long max_groups;   // a pass that pairs groups refuses to start when its groups
+                                     // could exceed this: min(grow_bound, n << nx) > max_groups
     unsigned long long range;        // list entries per resolve range (power of two, >= 32)
     PruneBits prune;
+    uint32_t q1, q2;                 // the cross-group qubits (kNoQubit when absent)
+    unsigned long long grow_bound;   // groups the state can hold after the pass, at most
 };
 
 }  // namespace sqc

@@ -42,7 +42,7 @@ class Options(ctypes.Structure):
                 ("load_factor", ctypes.c_double), ("initial_buckets", ctypes.c_uint64),
                 ("stream", ctypes.c_void_p), ("device", ctypes.c_uint32),
                 ("max_fused_gates", ctypes.c_uint32), ("time_passes", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("max_cross_qubits", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -194,7 +194,7 @@ class State:
     """A sparse statevector of ``nq`` qubits on one GPU, starting in |0...0>."""
 
     def __init__(self, nq, precision=FP64, prune_threshold=1e-14, load_factor=0.5, initial_buckets=0,
-                 stream=None, device=0, max_fused_gates=0, params=None, time_passes=False):
+                 stream=None, device=0, max_fused_gates=0, params=None, time_passes=False, max_cross_qubits=0):
         self._L = load()
         o = Options()
         self._L.sqc_default_options(ctypes.byref(o))
@@ -206,6 +206,7 @@ class State:
         o.device = device
         o.max_fused_gates = max_fused_gates
         o.time_passes = 1 if time_passes else 0
+        o.max_cross_qubits = max_cross_qubits
         h = ctypes.c_void_p()
         pp = ctypes.byref(params) if params is not None else None
         rc = self._L.sqc_create(nq, pp, ctypes.byref(o), ctypes.byref(h))

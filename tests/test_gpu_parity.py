@@ -70,6 +70,22 @@ def test_random_circuits_bitexact_staged_path(seed, precision):
     assert stats["amp_updates"] == upd
 
 
+@pytest.mark.parametrize("buckets", [64, STAGED_BUCKETS])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_pair_and_quad_passes_agree(buckets, precision):
+    """Passes pairing across one or two high qubits give the same bits as each other and as
+    the oracle, on the direct (small table) and the staged (large table) kernels."""
+    rng = circuits.SplitMix64(circuits.stream_seed("quad", buckets, precision))
+    g = circuits.random_circuit(36, 11, 400, 2, rng, kinds=ALL_KINDS)
+    got1, s1 = run_gpu(36, g, precision, initial_buckets=buckets, max_cross_qubits=1)
+    got2, s2 = run_gpu(36, g, precision, initial_buckets=buckets, max_cross_qubits=2)
+    want, upd = run_oracle(g, precision)
+    assert_identical(got1, want)
+    assert_identical(got2, want)
+    assert s1["amp_updates"] == s2["amp_updates"] == upd
+    assert s2["passes"] < s1["passes"]
+
+
 def test_growth_from_direct_into_staged_tables():
     """A state that outgrows 2^20 buckets moves from direct to staged passes mid-circuit."""
     rng = circuits.SplitMix64(circuits.stream_seed("grow-staged"))

@@ -1,0 +1,120 @@
+"""Host-side planning and memory bookkeeping, on the CPU (no GPU needed).
+
+A small C++ program is compiled against sparqc_gb300/csrc/sqc_plan.{h,cpp} and sqc_pool.h
+and run here: it checks how gates are resolved against the known key bits, how descriptor
+sequences are cut into passes with one or two cross-group qubits, the group bound that sizes
+batch slices, and the first-fit pool of the serving loop.
+"""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "sparqc_gb300", "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+
+PROGRAM = r'''
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include "sqc_plan.h"
+#include "sqc_pool.h"
+using namespace sqc;
+
+static int fails = 0;
+#define CHECK(c) do { if (!(c)) { std::printf("FAIL line %d: %s\n", __LINE__, #c); ++fails; } } while (0)
+
+static sqc_gate g(uint32_t kind, uint32_t t, uint64_t ctrl = 0, double th = 0.3) {
+    sqc_gate x; std::memset(&x, 0, sizeof x);
+    x.kind = kind; x.target = t; x.controls = ctrl; x.theta = th;
+    return x;
+}
+
+struct P { size_t g0, g1; uint32_t nx, q1, q2; bool fixed; };
+
+static std::vector<P> split(const std::vector<GateDesc>& d, uint32_t max_nx, size_t max_run = 64) {
+    std::vector<P> out;
+    split_passes(d.data(), d.size(), max_run, max_nx, [&](size_t a, size_t b, uint32_t nx, uint32_t q1, uint32_t q2, bool f) {
+        out.push_back(P{a, b, nx, q1, q2, f});
+    });
+    return out;
+}
+
+int main() {
+    // resolution against known bits: |0..0> knows every bit
+    Planner p;
+    GateDesc d;
+    CHECK(!plan_gate(p, g(KX, 7), &d));                 // uncontrolled X: frame flip
+    CHECK(p.frame == (1ULL << 7) && p.kval == (1ULL << 7));
+    CHECK(!plan_gate(p, g(KH, 3, 1ULL << 9), &d));       // control 9 known 0: identity
+    CHECK(p.credit == 2);
+    CHECK(plan_gate(p, g(KH, 3, 1ULL << 7), &d));        // control 7 known 1: dropped, H acts
+    CHECK(d.ctrl == 0 && d.kind == KH);
+    CHECK((p.kmask & (1ULL << 3)) == 0);                 // bit 3 now varies
+    CHECK(!plan_gate(p, g(KZ, 5), &d));                  // Z on a known-0 bit: identity
+    CHECK(plan_gate(p, g(KY, 6), &d) && d.kind == KYPH); // uncontrolled Y: relabel + diagonal
+    CHECK(group_bound(p, 20) == 1);                      // only bit 3 varies: one group
+    CHECK(plan_gate(p, g(KRX, 12), &d));
+    CHECK(plan_gate(p, g(KX, 13, 1ULL << 12), &d));      // controlled by a varying bit: on the device
+    CHECK(group_bound(p, 20) == 4);                      // bits 12, 13 vary
+    CHECK(std::strcmp(check_gate(g(KH, 20), 20), "target qubit out of range") == 0);
+    CHECK(check_gate(g(KH, 3, 1ULL << 3), 20) != nullptr);
+    CHECK(check_gate(g(KU, 19, 1ULL << 18), 20) == nullptr);
+
+    // pass split: gates on qubits 5, 6, 5, 7 with streamable gates in between
+    std::vector<GateDesc> s;
+    Planner q;
+    q.kmask = 0; q.kval = 0;                            // nothing known: every gate stays
+    for (auto gg : {g(KH, 5), g(KZ, 9), g(KH, 2), g(KRY, 6), g(KH, 5), g(KRX, 7), g(KT, 7), g(KH, 1)}) {
+        GateDesc x; CHECK(plan_gate(q, gg, &x)); s.push_back(x);
+    }
+    auto one = split(s, 1);
+    CHECK(one.size() == 4);
+    CHECK(one[0].g0 == 0 && one[0].g1 == 3 && one[0].nx == 1 && one[0].q1 == 5);
+    CHECK(one[1].g0 == 3 && one[1].g1 == 4 && one[1].q1 == 6);
+    CHECK(one[2].g0 == 4 && one[2].g1 == 5 && one[2].q1 == 5);
+    CHECK(one[3].g0 == 5 && one[3].g1 == 8 && one[3].q1 == 7 && one[3].nx == 1);
+    auto two = split(s, 2);
+    CHECK(two.size() == 2);
+    CHECK(two[0].g0 == 0 && two[0].g1 == 5 && two[0].nx == 2 && two[0].q1 == 5 && two[0].q2 == 6);
+    CHECK(two[1].g0 == 5 && two[1].g1 == 8 && two[1].nx == 1 && two[1].q1 == 7 && two[1].q2 == kNoQubit);
+    auto capped = split(s, 2, 2);                       // at most 2 gates per pass
+    CHECK(capped.size() == 4);
+    std::vector<GateDesc> diag;
+    for (auto gg : {g(KZ, 30), g(KRZ, 40), g(KT, 2)}) { GateDesc x; CHECK(plan_gate(q, gg, &x)); diag.push_back(x); }
+    auto dd = split(diag, 2);
+    CHECK(dd.size() == 1 && dd[0].nx == 0 && dd[0].fixed);
+
+    // first-fit pool with coalescing
+    RangePool pool;
+    pool.reset(1 << 20, 256);
+    size_t a = pool.alloc(1000), b = pool.alloc(5000), c = pool.alloc(300);
+    CHECK(a == 0 && b == 1024 && c == 1024 + 5120);
+    CHECK(pool.used() == 1024 + 5120 + 512);
+    pool.release(b, 5000);
+    CHECK(pool.alloc(6000) == 1024 + 5120 + 512);        // does not fit the hole: after c
+    size_t h = pool.alloc(4000);
+    CHECK(h == 1024);                                    // fits the hole
+    pool.release(a, 1000); pool.release(h, 4000); pool.release(c, 300);
+    pool.release(1024 + 5120 + 512, 6000);
+    CHECK(pool.used() == 0 && pool.largest_free() == (1u << 20));
+    CHECK(pool.alloc(2u << 20) == SIZE_MAX);
+
+    std::printf("fails=%d\n", fails);
+    return fails ? 1 : 0;
+}
+'''
+
+
+def test_planner_and_pool(tmp_path):
+    src = tmp_path / "planner.cpp"
+    src.write_text(PROGRAM)
+    exe = tmp_path / "planner"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", INCLUDE, "-I", CSRC, str(src),
+                        os.path.join(CSRC, "sqc_plan.cpp"), "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.fail(r.stderr)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert "fails=0" in out.stdout
