@@ -85,6 +85,7 @@ const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_
                      b.q1 = (uint8_t)(nx >= 1 ? q1 : 0xFF);
                      b.q2 = (uint8_t)(nx >= 2 ? q2 : 0xFF);
                      c.passes.push_back(b);
+                     encode_pass(c.desc.data(), g0, g1, q1);
                  });
     if (c.passes.size() > kMaxBatchPasses) return "too many passes for a batch circuit";
     c.bound = group_bound(p, nq);

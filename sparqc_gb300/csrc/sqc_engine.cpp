@@ -303,9 +303,6 @@ int Engine::flush() {
     gates_applied_ += n;
     pending_.clear();
     if (nd == 0) return SQC_OK;
-    if ((rc = cuda(cudaMemcpyAsync(d_desc_ + desc_used_, hd, nd * sizeof(GateDesc), cudaMemcpyHostToDevice, stream_),
-                   "H2D gate descriptors")))
-        return rc;
     PassArgs a;
     std::memset(&a, 0, sizeof a);
     a.t = dev();
@@ -314,8 +311,6 @@ int Engine::flush() {
     a.amp_bytes = dbl_ ? 16u : 8u;
     a.max_groups = max_groups();
     a.prune = prune_;
-    cudaEvent_t ev_prev = nullptr;
-    if (time_passes_ && (rc = record_event(&ev_prev))) return rc;
     struct Span {
         size_t g0, g1;
         uint32_t nx, q1, q2;
@@ -324,7 +319,13 @@ int Engine::flush() {
     std::vector<Span> spans;
     split_passes(hd, nd, max_run_, max_nx_, [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, bool fixed) {
         spans.push_back(Span{g0, g1, nx, q1, q2, fixed});
+        encode_pass(hd, g0, g1, q1);
     });
+    if ((rc = cuda(cudaMemcpyAsync(d_desc_ + desc_used_, hd, nd * sizeof(GateDesc), cudaMemcpyHostToDevice, stream_),
+                   "H2D gate descriptors")))
+        return rc;
+    cudaEvent_t ev_prev = nullptr;
+    if (time_passes_ && (rc = record_event(&ev_prev))) return rc;
     for (const Span& sp : spans) {
         const size_t i = sp.g1;
         a.g0 = (uint32_t)sp.g0;

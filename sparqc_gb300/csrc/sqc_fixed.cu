@@ -29,6 +29,7 @@
 
 #include "../../include/sparqc.h"
 #include "sqc_kernels.h"
+#include "sqc_plan.h"
 
 namespace sqc {
 namespace {
@@ -153,6 +154,26 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     if (launch_set_state(reinterpret_cast<const unsigned long long*>(keys_in), re_in, im_in, n_in, t, ctl, true,
                          sms, st) != cudaSuccess)
         return SQC_ERR_CUDA;
+    // same pass split as the engine with one cross-group qubit per pass: one cross-group gate,
+    // then a stream run; each pass's gates are encoded before the descriptors are uploaded
+    struct Span {
+        uint32_t g0, g1, q1;
+        bool pair, fixed;
+    };
+    Span spans[kFixedMaxGates];
+    size_t ns = 0, i = 0;
+    while (i < n_gates) {
+        const size_t start = i;
+        auto streamable = [&](size_t k) { return hd[k].target < (uint32_t)kSlotBits || diag_kind(hd[k].kind); };
+        const bool pair = !streamable(i);
+        if (pair) ++i;
+        while (i < n_gates && i - start < (size_t)kMaxRun && streamable(i)) ++i;
+        bool fixed = true;
+        for (size_t k = start; k < i; ++k) fixed = fixed && diag_kind(hd[k].kind);
+        const uint32_t q1 = pair ? hd[start].target : kNoQubit;
+        encode_pass(hd, start, i, q1);
+        spans[ns++] = Span{(uint32_t)start, (uint32_t)i, q1, pair, fixed};
+    }
     if (n_gates && cudaMemcpyAsync(d_desc, hd, n_gates * sizeof(GateDesc), cudaMemcpyHostToDevice, st) != cudaSuccess)
         return SQC_ERR_CUDA;
 
@@ -169,22 +190,14 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     float tf = (float)thr;
     if ((double)tf >= thr) tf = std::nextafter(tf, 0.0f);
     std::memcpy(&a.prune.f, &tf, sizeof(float));
-    size_t i = 0;
-    while (i < n_gates) {   // same pass split as the engine: one cross-group gate, then a stream run
-        const size_t start = i;
-        auto streamable = [&](size_t k) { return hd[k].target < (uint32_t)kSlotBits || diag_kind(hd[k].kind); };
-        const bool pair = !streamable(i);
-        if (pair) ++i;
-        while (i < n_gates && i - start < (size_t)kMaxRun && streamable(i)) ++i;
-        bool fixed = true;
-        for (size_t k = start; k < i; ++k) fixed = fixed && diag_kind(hd[k].kind);
-        a.g0 = (uint32_t)start;
-        a.g1 = (uint32_t)i;
-        a.nx = pair ? 1u : 0u;
-        a.q1 = pair ? hd[start].target : kNoQubit;
+    for (size_t k = 0; k < ns; ++k) {
+        a.g0 = spans[k].g0;
+        a.g1 = spans[k].g1;
+        a.nx = spans[k].pair ? 1u : 0u;
+        a.q1 = spans[k].q1;
         a.q2 = kNoQubit;
         a.grow_bound = ~0ULL;
-        a.keys_fixed = fixed ? 1u : 0u;
+        a.keys_fixed = spans[k].fixed ? 1u : 0u;
         if (launch_pass(a, kFixedBuckets, true, sms, st) < 0) return SQC_ERR_CUDA;
     }
     if (launch_readout(t, ctl, kFixedBuckets, 0ULL, true, reinterpret_cast<unsigned long long*>(keys_out), re_out,

@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
             const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
             load_val_g<T>(t, va, Ga, ba, j);
             load_val_g<T>(t, vb, Gb, bb, j);
-            run_gates<T>(a.gates, a.g0, a.g1, kNoQubit, kNoQubit, va, vb, lane, a.prune, upd);
+            run_gates<T>(a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
             write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
             write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         }
@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
             long long mb;
             unsigned long long G0;
             const unsigned om = units4<NX>(t, ep, e0, n, m1, m2, lane, &mb, &G0);
-            run_units4<T, NX>(t, ep, ctl, a.gates, a.g0, a.g1, a.q1, a.q2, m1, m2, om, mb, G0, lane, a.prune, va, vb,
-                              cnt_nnz, cnt_empty, upd);
+            run_units4<T, NX>(t, ep, ctl, a.gates, a.g0, a.g1, m1, m2, om, mb, G0, lane, a.prune, va, vb, cnt_nnz,
+                              cnt_empty, upd);
         }
     }
     finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
@@ -315,7 +315,6 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
     const unsigned long long R = a.range;
     const unsigned long long m1 = NX ? 1ULL << (a.q1 - kSlotBits) : 0ULL;
     const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
-    const uint32_t q1 = NX ? a.q1 : kNoQubit, q2 = NX == 2 ? a.q2 : kNoQubit;
     SlotSource src;
     src.next = gw;
     src.stride = nw;
@@ -349,7 +348,7 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
         load_val_s<T>(va, Ga, ba, sl, ka, jj);
         load_val_s<T>(vb, Gb, bb, sl, kb, jj);
         __syncwarp();
-        run_gates<T>(a.gates, a.g0, a.g1, q1, q2, va, vb, lane, a.prune, upd);
+        run_gates<T>(a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         if (NX) append_new(t, ctl, fa, fb, lane);

@@ -36,11 +36,11 @@ template <class T> struct Val {
 };
 
 struct GateHead {
-    uint32_t kind, target, flip, credit;
+    uint32_t kind, target, op, credit;
     unsigned long long ctrl, cval;
 };
 
-// The descriptor's first 32 bytes in two vector loads: {kind, target, ctrl}, {cval, flip, pad}.
+// The descriptor's first 32 bytes in two vector loads: {kind, target, ctrl}, {cval, op, credit}.
 __device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
     const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(g));
     const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(g) + 1);
@@ -49,65 +49,82 @@ __device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
     h.target = v0.y;
     h.ctrl = (unsigned long long)v0.z | ((unsigned long long)v0.w << 32);
     h.cval = (unsigned long long)v1.x | ((unsigned long long)v1.y << 32);
-    h.flip = v1.z;
+    h.op = v1.z;
     h.credit = v1.w;
     return h;
 }
 
-// One streamable gate on one held slot. `off` is the lane distance to the partner slot
-// (1 << q for q < 4, inside the half-warp) or 0 for a diagonal gate on a qubit >= 4.
+// FP64 arithmetic issues on the slow FP64 pipe: skip it when no lane of the warp needs it.
+// FP32 arithmetic is cheaper than the vote.
+template <class T> struct Vote { static constexpr bool kSkip = sizeof(T) == 8; };
+
 template <class T>
-__device__ __forceinline__ void gate_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
+__device__ __forceinline__ bool warp_needs(bool need) {
+    return Vote<T>::kSkip ? __any_sync(kFull, need) : true;
+}
+
+// Whether the gate acts on the slot's key (its controls hold) and the slot's logical target bit.
+__device__ __forceinline__ bool slot_sat(const GateHead& h, unsigned long long G, int j) {
+    if (!(h.op & kOpCtrl)) return true;
+    const unsigned long long key = (G << kSlotBits) | (unsigned long long)j;
+    return (key & h.ctrl) == h.cval;
+}
+
+__device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long G, int j) {
+    const unsigned b = (h.op & kOpLowBit) ? ((unsigned)j >> h.target) & 1u
+                                          : (unsigned)(G >> (h.target - kSlotBits)) & 1u;
+    return (b ^ (h.op & kOpFlip)) != 0;
+}
+
+// A branching or swap gate whose partner slot sits in lane ^ off.
+template <class T>
+__device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
                                           const PruneBits& pb) {
-    const unsigned long long key = (v.G << kSlotBits) | (unsigned long long)j;
-    const bool sat = (key & h.ctrl) == h.cval;
-    const bool bit = (((key >> h.target) & 1ULL) != 0) != (h.flip != 0);
-    if (off) {
-        Cx<T> pa;
-        pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
-        pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
-        const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
-        if (is_swap(h.kind)) {
-            if (sat) {
-                v.amp = swap_update<T>(h.kind, bit, pa);
-                v.pres = pp;
-                v.dirty = true;
-            }
-        } else if (is_branch(h.kind)) {
-            const bool any = v.pres || pp;
-            if (__any_sync(kFull, sat && any)) {
-                const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
-                if (sat) {
-                    const bool keep = any && !negligible(o, pb);
-                    v.pres = keep;
-                    v.amp = keep ? o : czero<T>();
-                    v.dirty = true;
-                }
-            }
-        } else {
-            const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
-            if (__any_sync(kFull, need)) {
-                const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
-                if (need) { v.amp = o; v.dirty = true; }
-            }
+    const bool sat = slot_sat(h, v.G, j);
+    const bool bit = slot_bit(h, v.G, j);
+    Cx<T> pa;
+    pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
+    pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
+    const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
+    if (h.op & kOpSwap) {
+        if (sat) {
+            v.amp = swap_update<T>(h.kind, bit, pa);
+            v.pres = pp;
+            v.dirty = true;
         }
         return;
     }
-    const bool need = sat && v.pres && (bit || !is_one_sided(h.kind));
-    if (__any_sync(kFull, need)) {
+    const bool any = v.pres || pp;
+    if (warp_needs<T>(sat && any)) {
+        const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
+        if (sat) {
+            const bool keep = any && !negligible(o, pb);
+            v.pres = keep;
+            v.amp = keep ? o : czero<T>();
+            v.dirty = true;
+        }
+    }
+}
+
+// A diagonal gate on one slot (lane-local).
+template <class T>
+__device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, Val<T>& v, int j) {
+    const bool bit = slot_bit(h, v.G, j);
+    const bool need = v.pres && (bit || !(h.op & kOpOneSided)) && slot_sat(h, v.G, j);
+    if (warp_needs<T>(need)) {
         const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
         if (need) { v.amp = o; v.dirty = true; }
     }
 }
 
-// The cross-group gate of a pair pass, lane-local: a = slot of G0 (stored bit 0), b = slot of G1.
+// A branching or swap gate on the pass's first cross-group qubit, lane-local: a = slot of the
+// group with stored target bit 0, b = slot of its partner group.
 template <class T>
 __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b, int j,
                                           const PruneBits& pb) {
-    const unsigned long long key = (a.G << kSlotBits) | (unsigned long long)j;
-    const bool sat = (key & h.ctrl) == h.cval;
-    const bool bit_a = h.flip != 0, bit_b = !bit_a;
-    if (is_swap(h.kind)) {
+    const bool sat = slot_sat(h, a.G, j);
+    const bool bit_a = (h.op & kOpFlip) != 0, bit_b = !bit_a;
+    if (h.op & kOpSwap) {
         if (sat) {
             const Cx<T> na = swap_update<T>(h.kind, bit_a, b.amp), nb = swap_update<T>(h.kind, bit_b, a.amp);
             const bool pa = b.pres, pbr = a.pres;
@@ -118,7 +135,7 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
         return;
     }
     const bool any = a.pres || b.pres;
-    if (__any_sync(kFull, sat && any)) {
+    if (warp_needs<T>(sat && any)) {
         const Cx<T> oa = branch_update<T>(h.kind, g, bit_a, a.amp, b.amp);
         const Cx<T> ob = branch_update<T>(h.kind, g, bit_b, b.amp, a.amp);
         if (sat) {
@@ -130,16 +147,16 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
     }
 }
 
-// Apply gates [g0, g1) to the two held slots. Branching and swap gates on the pass's first
-// cross-group qubit q1 pair a with b (lane-local); those on the second one, q2, pair each lane
-// with lane ^ 16 (the other half holds the groups with the q2 bit set); every other gate acts
-// within a group (warp shuffle for qubits 0..3, lane-local for diagonal gates). Stream passes pass q1 = q2 =
-// kNoQubit. Lane 0 accumulates the amp-update count: every gate is credited with the present
-// slots it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
+// Apply gates [g0, g1) to the two held slots, each as its pass encoded it (encode_pass):
+// branching and swap gates on the pass's first cross-group qubit pair a with b (lane-local),
+// those on qubits 0..3 or on the second cross-group qubit pair each lane with lane ^ off
+// (the other half of the warp holds the groups with the second qubit's bit set), diagonal
+// gates are lane-local. Lane 0 accumulates the amp-update count: every gate is credited with
+// the present slots it sees, and host-resolved gates recorded in a descriptor's credit with
+// the same count.
 template <class T>
-__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, uint32_t q1,
-                                          uint32_t q2, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
-                                          unsigned long long& upd) {
+__device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, Val<T>& a,
+                                          Val<T>& b, int lane, const PruneBits& pb, unsigned long long& upd) {
     const int j = lane & 15;
     // present slots in the warp: only a branching gate changes the count (swap gates permute
     // presence among slots that satisfy the same controls, diagonal gates keep it)
@@ -149,16 +166,18 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
         const GateDesc* g = gates + gi;
         const GateHead h = gate_head(g);
         if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
-        recount = is_branch(h.kind);
+        recount = (h.op & kOpBranch) != 0;
         if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
-        const bool cross = is_branch(h.kind) || is_swap(h.kind);
-        if (cross && h.target == q1) {
+        if (h.op & kOpPair) {
             pair_step<T>(g, h, a, b, j, pb);
-            continue;
+        } else if (h.op & kOpShfl) {
+            const int off = 1 << ((h.op >> kOpOffShift) & 7u);
+            shfl_step<T>(g, h, off, a, j, pb);
+            shfl_step<T>(g, h, off, b, j, pb);
+        } else {
+            diag_step<T>(g, h, a, j);
+            diag_step<T>(g, h, b, j);
         }
-        const int off = h.target < (uint32_t)kSlotBits ? (1 << h.target) : (cross && h.target == q2 ? 16 : 0);
-        gate_step<T>(g, h, off, a, j, pb);
-        gate_step<T>(g, h, off, b, j, pb);
     }
 }
 
@@ -296,8 +315,8 @@ __device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsig
 // table, the gates applied, and the slots written back.
 template <class T, int NX>
 __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates, uint32_t g0,
-                                           uint32_t g1, uint32_t q1, uint32_t q2, unsigned long long m1,
-                                           unsigned long long m2, unsigned om, long long mb, unsigned long long G0,
+                                           uint32_t g1, unsigned long long m1, unsigned long long m2, unsigned om,
+                                           long long mb, unsigned long long G0,
                                            int lane, const PruneBits& pb, Val<T>& va, Val<T>& vb,
                                            unsigned long long& cnt_nnz, unsigned long long& cnt_empty,
                                            unsigned long long& upd) {
@@ -326,7 +345,7 @@ __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* 
         const bool act = u >= 0;
         load_val_g<T>(t, va, Ga, act ? xa : -1, j);
         load_val_g<T>(t, vb, Ga | m1, act ? xb : -1, j);
-        run_gates<T>(gates, g0, g1, q1, NX == 2 ? q2 : kNoQubit, va, vb, lane, pb, upd);
+        run_gates<T>(gates, g0, g1, va, vb, lane, pb, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         append_new(t, ctl, fa, fb, lane);

@@ -70,6 +70,30 @@ bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out) {
     return true;
 }
 
+void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1) {
+    for (size_t k = g0; k < g1; ++k) {
+        GateDesc& g = d[k];
+        uint32_t op = g.flip & kOpFlip;
+        const bool branch = is_branch_kind(g.kind), swap = is_swap_kind(g.kind);
+        if (g.ctrl) op |= kOpCtrl;
+        if (branch) op |= kOpBranch;
+        if (swap) op |= kOpSwap;
+        if (is_one_sided_kind(g.kind)) op |= kOpOneSided;
+        if (g.target < (uint32_t)kSlotBits) op |= kOpLowBit;
+        if (branch || swap) {
+            if (g.target == q1 && g.target >= (uint32_t)kSlotBits) {
+                op |= kOpPair;
+            } else {
+                // qubits 0..3: a lane of the same half; the pass's second cross-group qubit:
+                // the other half of the warp
+                const uint32_t off_log2 = g.target < (uint32_t)kSlotBits ? g.target : 4u;
+                op |= kOpShfl | (off_log2 << kOpOffShift);
+            }
+        }
+        g.flip = op;
+    }
+}
+
 unsigned long long group_bound(const Planner& p, uint32_t nq) {
     const unsigned long long reg = nq >= 64 ? ~0ULL : ((1ULL << nq) - 1);
     const unsigned long long var = ~p.kmask & reg & ~15ULL;

@@ -72,6 +72,11 @@ void split_passes(const GateDesc* d, size_t n, size_t max_run, uint32_t max_nx, 
     }
 }
 
+// Record in descriptors [g0, g1) -- one pass, whose first cross-group qubit is q1 -- how the
+// pass applies each gate (GateDesc.flip kOp* bits). Cross-group gates on another qubit >= 4
+// are on the pass's second cross-group qubit.
+void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1);
+
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose
 // planning ended in p (starting from keys that agreed on every bit of the starting kmask):
 // 2^(bits >= 4 that have ever differed between keys).

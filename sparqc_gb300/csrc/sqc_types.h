@@ -74,7 +74,8 @@ struct Ctl {
 // device and the CPU oracle use identical values) in the stored-key frame: the gate acts on
 // a stored key s iff (s & ctrl) == cval, and the member's logical target bit is
 // ((s >> target) & 1) ^ flip. The first 32 bytes (kind .. pad) are read as two 16-byte
-// vectors, hence the alignment.
+// vectors, hence the alignment. `flip` holds the frame flip in bit 0 and, once the gate's
+// pass is known, how that pass applies it (kOp* bits, set by encode_pass on the host).
 struct alignas(16) GateDesc {
     uint32_t kind, target;
     unsigned long long ctrl, cval;
@@ -84,6 +85,17 @@ struct alignas(16) GateDesc {
     float cf, sf;         // float copies for FP32 states
     float mf[8];
 };
+
+// GateDesc.flip bits.
+constexpr uint32_t kOpFlip = 1u << 0;      // the stored frame flips the target bit
+constexpr uint32_t kOpPair = 1u << 1;      // pairs the a and b slots (first cross-group qubit)
+constexpr uint32_t kOpShfl = 1u << 2;      // partner slot in lane ^ (1 << off_log2)
+constexpr uint32_t kOpOffShift = 3;        // off_log2: bits 3..5
+constexpr uint32_t kOpCtrl = 1u << 6;      // controls to test per key
+constexpr uint32_t kOpBranch = 1u << 7;    // H, Rx, Ry, U
+constexpr uint32_t kOpSwap = 1u << 8;      // X, Y
+constexpr uint32_t kOpOneSided = 1u << 9;  // diagonal gate that leaves bit-0 keys unchanged
+constexpr uint32_t kOpLowBit = 1u << 10;   // target < 4: the target bit is in the slot index
 
 struct PruneBits {
     unsigned long long d;   // bit pattern of thr (double)
