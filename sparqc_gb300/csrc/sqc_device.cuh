@@ -169,86 +169,73 @@ template <> struct Coef<float> {
     __device__ static __forceinline__ float m(const GateDesc* g, int i) { return __ldg(&g->mf[i]); }
 };
 
-// Branching update seen from one member of a pair: a = own amplitude, b = partner amplitude,
-// bit = own logical target bit. Each form rounds exactly like the reference's pair formula
-// for that member (a + (-b) == a - b and (-s)*x == -(s*x) hold exactly in IEEE arithmetic):
+// Branching update seen from one member of a pair, for gate kind K: a = own amplitude,
+// b = partner amplitude, bit = own logical target bit. Each form rounds exactly like the
+// reference's pair formula for that member (a + (-b) == a - b and (-s)*x == -(s*x) hold
+// exactly in IEEE arithmetic):
 //   H : bit 0 -> f*(v0 + v1),             bit 1 -> f*(v0 - v1)
 //   Rx: c*own + s*(i-rotated partner)      (symmetric in the two members)
 //   Ry: bit 0 -> c*v0 - s*v1,             bit 1 -> c*v1 + s*v0
 //   U : self term first, then partner term, fused multiply-add chain (no reference form).
-template <class T>
-__device__ __forceinline__ Cx<T> branch_update(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
+template <class T, uint32_t K>
+__device__ __forceinline__ Cx<T> branch_update(const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
     using A = Arith<T>;
     Cx<T> o;
-    switch (kind) {
-    case KH: {
+    if constexpr (K == KH) {
         const T f = Coef<T>::c(g);
         const Cx<T> x = bit ? b : a;
         const Cx<T> y = bit ? Cx<T>{neg(a.r), neg(a.i)} : b;
         o.r = A::mul(f, A::add(x.r, y.r));
         o.i = A::mul(f, A::add(x.i, y.i));
-        break;
-    }
-    case KRX: {
+    } else if constexpr (K == KRX) {
         const T c = Coef<T>::c(g), s = Coef<T>::s(g);
         o.r = A::add(A::mul(c, a.r), A::mul(s, b.i));
         o.i = A::sub(A::mul(c, a.i), A::mul(s, b.r));
-        break;
-    }
-    case KRY: {
+    } else if constexpr (K == KRY) {
         const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
         const T s = bit ? s0 : neg(s0);
         o.r = A::add(A::mul(c, a.r), A::mul(s, b.r));
         o.i = A::add(A::mul(c, a.i), A::mul(s, b.i));
-        break;
-    }
-    default: {  // KU
+    } else {  // KU
         const T m00r = Coef<T>::m(g, 0), m00i = Coef<T>::m(g, 1), m01r = Coef<T>::m(g, 2), m01i = Coef<T>::m(g, 3);
         const T m10r = Coef<T>::m(g, 4), m10i = Coef<T>::m(g, 5), m11r = Coef<T>::m(g, 6), m11i = Coef<T>::m(g, 7);
         const T msr = bit ? m11r : m00r, msi = bit ? m11i : m00i;
         const T mor = bit ? m10r : m01r, moi = bit ? m10i : m01i;
         o.r = A::fma(neg(moi), b.i, A::fma(mor, b.r, A::fma(neg(msi), a.i, A::mul(msr, a.r))));
         o.i = A::fma(moi, b.r, A::fma(mor, b.i, A::fma(msi, a.r, A::mul(msr, a.i))));
-        break;
-    }
     }
     return o;
 }
 
-// Diagonal update of one amplitude (reference: z_core, phase_core, rz_core).
-template <class T>
-__device__ __forceinline__ Cx<T> diag_update(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a) {
+// Diagonal update of one amplitude for gate kind K (reference: z_core, phase_core, rz_core).
+template <class T, uint32_t K>
+__device__ __forceinline__ Cx<T> diag_update(const GateDesc* g, bool bit, Cx<T> a) {
     using A = Arith<T>;
-    switch (kind) {
-    case KZ: return bit ? Cx<T>{neg(a.r), neg(a.i)} : a;
-    case KS: return bit ? Cx<T>{neg(a.i), a.r} : a;
-    case KSDG: return bit ? Cx<T>{a.i, neg(a.r)} : a;
-    case KYPH: return bit ? Cx<T>{neg(a.i), a.r} : Cx<T>{a.i, neg(a.r)};
-    case KRZ: {
+    if constexpr (K == KZ) return bit ? Cx<T>{neg(a.r), neg(a.i)} : a;
+    else if constexpr (K == KS) return bit ? Cx<T>{neg(a.i), a.r} : a;
+    else if constexpr (K == KSDG) return bit ? Cx<T>{a.i, neg(a.r)} : a;
+    else if constexpr (K == KYPH) return bit ? Cx<T>{neg(a.i), a.r} : Cx<T>{a.i, neg(a.r)};
+    else if constexpr (K == KRZ) {
         const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
         const T s = bit ? s0 : neg(s0);   // bit 0: conj(a)*v0, bit 1: a*v1
         return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
-    }
-    default: {  // KPHASE, KT, KTDG
-        if (!bit) return a;
+    } else {  // KPHASE, KT, KTDG: only bit-1 amplitudes change (callers skip bit 0)
         const T c = Coef<T>::c(g), s = Coef<T>::s(g);
         return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
     }
-    }
 }
 
-// Swap update: the amplitude arriving from the partner (reference: x_core, y_core).
-template <class T>
-__device__ __forceinline__ Cx<T> swap_update(uint32_t kind, bool bit, Cx<T> b) {
-    if (kind == KX) return b;
-    return bit ? Cx<T>{neg(b.i), b.r} : Cx<T>{b.i, neg(b.r)};   // Y
+// Swap update for gate kind K: the amplitude arriving from the partner (reference: x_core,
+// y_core).
+template <class T, uint32_t K>
+__device__ __forceinline__ Cx<T> swap_update(bool bit, Cx<T> b) {
+    if constexpr (K == KX) return b;
+    else return bit ? Cx<T>{neg(b.i), b.r} : Cx<T>{b.i, neg(b.r)};   // Y
 }
 
-__device__ __forceinline__ bool is_branch(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
-__device__ __forceinline__ bool is_swap(uint32_t k) { return k == KX || k == KY; }
-// Diagonal kinds whose bit-0 member is unchanged: the whole warp can skip them when no lane
-// holds a satisfied bit-1 member.
-__device__ __forceinline__ bool is_one_sided(uint32_t k) {
+__host__ __device__ constexpr bool branch_kind(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
+__host__ __device__ constexpr bool swap_kind(uint32_t k) { return k == KX || k == KY; }
+__host__ __device__ constexpr bool one_sided_kind(uint32_t k) {
     return k == KZ || k == KS || k == KSDG || k == KPHASE || k == KT || k == KTDG;
 }
 

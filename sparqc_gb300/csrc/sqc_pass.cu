@@ -194,7 +194,7 @@ template <class T> struct Slot {
 template <class T>
 __device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsigned b, const Slot<T>& sl, int k,
                                            int j) {
-    v.G = G;
+    v.key = (G << kSlotBits) | (unsigned long long)j;
     v.b = b == kNoBucket ? -1 : (long long)b;
     v.dirty = false;
     v.pres = false;

@@ -26,10 +26,10 @@ __device__ __forceinline__ void store_amp(void* amps, size_t s, Cx<T> a) {
 
 __device__ __forceinline__ bool slot_present(unsigned long long key, int j) { return (int)(key & 15ULL) == j; }
 
-// One slot held by a lane: its group, amplitude and presence, where it lives (b = -1 for a
-// group absent at the start of the pass) and whether the pass changed it.
+// One slot held by a lane: its key ((group << 4) | slot), amplitude and presence, where it
+// lives (b = -1 for a group absent at the start of the pass) and whether the pass changed it.
 template <class T> struct Val {
-    unsigned long long G;
+    unsigned long long key;
     long long b;
     Cx<T> amp;
     bool pres, pres0, dirty;
@@ -64,100 +64,113 @@ __device__ __forceinline__ bool warp_needs(bool need) {
 }
 
 // Whether the gate acts on the slot's key (its controls hold) and the slot's logical target bit.
-__device__ __forceinline__ bool slot_sat(const GateHead& h, unsigned long long G, int j) {
-    if (!(h.op & kOpCtrl)) return true;
-    const unsigned long long key = (G << kSlotBits) | (unsigned long long)j;
-    return (key & h.ctrl) == h.cval;
+__device__ __forceinline__ bool slot_sat(const GateHead& h, unsigned long long key) {
+    return !(h.op & kOpCtrl) || (key & h.ctrl) == h.cval;
 }
 
-__device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long G, int j) {
-    const unsigned b = (h.op & kOpLowBit) ? ((unsigned)j >> h.target) & 1u
-                                          : (unsigned)(G >> (h.target - kSlotBits)) & 1u;
-    return (b ^ (h.op & kOpFlip)) != 0;
+__device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long key) {
+    return (((unsigned)(key >> h.target) ^ h.op) & 1u) != 0;   // kOpFlip is bit 0
 }
 
-// A branching or swap gate whose partner slot sits in lane ^ off.
-template <class T>
-__device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v, int j,
+// A branching or swap gate of kind K whose partner slot sits in lane ^ off.
+template <class T, uint32_t K>
+__device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v,
                                           const PruneBits& pb) {
-    const bool sat = slot_sat(h, v.G, j);
-    const bool bit = slot_bit(h, v.G, j);
+    const bool sat = slot_sat(h, v.key);
+    const bool bit = slot_bit(h, v.key);
     Cx<T> pa;
     pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
     pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
     const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
-    if (h.op & kOpSwap) {
+    if constexpr (swap_kind(K)) {
         if (sat) {
-            v.amp = swap_update<T>(h.kind, bit, pa);
+            v.amp = swap_update<T, K>(bit, pa);
             v.pres = pp;
             v.dirty = true;
         }
-        return;
-    }
-    const bool any = v.pres || pp;
-    if (warp_needs<T>(sat && any)) {
-        const Cx<T> o = branch_update<T>(h.kind, g, bit, v.amp, pa);
-        if (sat) {
-            const bool keep = any && !negligible(o, pb);
-            v.pres = keep;
-            v.amp = keep ? o : czero<T>();
-            v.dirty = true;
+    } else {
+        const bool any = v.pres || pp;
+        if (warp_needs<T>(sat && any)) {
+            const Cx<T> o = branch_update<T, K>(g, bit, v.amp, pa);
+            if (sat) {
+                const bool keep = any && !negligible(o, pb);
+                v.pres = keep;
+                v.amp = keep ? o : czero<T>();
+                v.dirty = true;
+            }
         }
     }
 }
 
-// A diagonal gate on one slot (lane-local).
-template <class T>
-__device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, Val<T>& v, int j) {
-    const bool bit = slot_bit(h, v.G, j);
-    const bool need = v.pres && (bit || !(h.op & kOpOneSided)) && slot_sat(h, v.G, j);
+// A diagonal gate of kind K on one slot (lane-local).
+template <class T, uint32_t K>
+__device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, Val<T>& v) {
+    const bool bit = slot_bit(h, v.key);
+    const bool need = v.pres && (!one_sided_kind(K) || bit) && slot_sat(h, v.key);
     if (warp_needs<T>(need)) {
-        const Cx<T> o = diag_update<T>(h.kind, g, bit, v.amp);
+        const Cx<T> o = diag_update<T, K>(g, bit, v.amp);
         if (need) { v.amp = o; v.dirty = true; }
     }
 }
 
-// A branching or swap gate on the pass's first cross-group qubit, lane-local: a = slot of the
-// group with stored target bit 0, b = slot of its partner group.
-template <class T>
-__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b, int j,
+// A branching or swap gate of kind K on the pass's first cross-group qubit, lane-local:
+// a = slot of the group with stored target bit 0, b = slot of its partner group.
+template <class T, uint32_t K>
+__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b,
                                           const PruneBits& pb) {
-    const bool sat = slot_sat(h, a.G, j);
+    const bool sat = slot_sat(h, a.key);
     const bool bit_a = (h.op & kOpFlip) != 0, bit_b = !bit_a;
-    if (h.op & kOpSwap) {
+    if constexpr (swap_kind(K)) {
         if (sat) {
-            const Cx<T> na = swap_update<T>(h.kind, bit_a, b.amp), nb = swap_update<T>(h.kind, bit_b, a.amp);
+            const Cx<T> na = swap_update<T, K>(bit_a, b.amp), nb = swap_update<T, K>(bit_b, a.amp);
             const bool pa = b.pres, pbr = a.pres;
             a.amp = na; b.amp = nb;
             a.pres = pa; b.pres = pbr;
             a.dirty = b.dirty = true;
         }
-        return;
-    }
-    const bool any = a.pres || b.pres;
-    if (warp_needs<T>(sat && any)) {
-        const Cx<T> oa = branch_update<T>(h.kind, g, bit_a, a.amp, b.amp);
-        const Cx<T> ob = branch_update<T>(h.kind, g, bit_b, b.amp, a.amp);
-        if (sat) {
-            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
-            a.pres = ka; a.amp = ka ? oa : czero<T>();
-            b.pres = kb; b.amp = kb ? ob : czero<T>();
-            a.dirty = b.dirty = true;
+    } else {
+        const bool any = a.pres || b.pres;
+        if (warp_needs<T>(sat && any)) {
+            const Cx<T> oa = branch_update<T, K>(g, bit_a, a.amp, b.amp);
+            const Cx<T> ob = branch_update<T, K>(g, bit_b, b.amp, a.amp);
+            if (sat) {
+                const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+                a.pres = ka; a.amp = ka ? oa : czero<T>();
+                b.pres = kb; b.amp = kb ? ob : czero<T>();
+                a.dirty = b.dirty = true;
+            }
         }
     }
 }
 
-// Apply gates [g0, g1) to the two held slots, each as its pass encoded it (encode_pass):
+// One gate of kind K on the lane's two slots, as its pass encoded it (encode_pass).
+template <class T, uint32_t K>
+__device__ __forceinline__ void gate_on(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b,
+                                        const PruneBits& pb) {
+    if constexpr (branch_kind(K) || swap_kind(K)) {
+        if (h.op & kOpPair) {
+            pair_step<T, K>(g, h, a, b, pb);
+        } else {
+            const int off = 1 << ((h.op >> kOpOffShift) & 7u);
+            shfl_step<T, K>(g, h, off, a, pb);
+            shfl_step<T, K>(g, h, off, b, pb);
+        }
+    } else {
+        diag_step<T, K>(g, h, a);
+        diag_step<T, K>(g, h, b);
+    }
+}
+
+// Apply gates [g0, g1) to the two held slots. Each gate is dispatched once on its (warp-
+// uniform) kind to code specialised for that kind, and applied as its pass encoded it:
 // branching and swap gates on the pass's first cross-group qubit pair a with b (lane-local),
-// those on qubits 0..3 or on the second cross-group qubit pair each lane with lane ^ off
-// (the other half of the warp holds the groups with the second qubit's bit set), diagonal
-// gates are lane-local. Lane 0 accumulates the amp-update count: every gate is credited with
-// the present slots it sees, and host-resolved gates recorded in a descriptor's credit with
-// the same count.
+// those on qubits 0..3 or on the second cross-group qubit pair each lane with lane ^ off (the
+// other half of the warp holds the groups with the second qubit's bit set), diagonal gates are
+// lane-local. Lane 0 accumulates the amp-update count: every gate is credited with the present
+// slots it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
 template <class T>
 __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, Val<T>& a,
                                           Val<T>& b, int lane, const PruneBits& pb, unsigned long long& upd) {
-    const int j = lane & 15;
     // present slots in the warp: only a branching gate changes the count (swap gates permute
     // presence among slots that satisfy the same controls, diagonal gates keep it)
     unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
@@ -168,15 +181,21 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
         if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
         recount = (h.op & kOpBranch) != 0;
         if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
-        if (h.op & kOpPair) {
-            pair_step<T>(g, h, a, b, j, pb);
-        } else if (h.op & kOpShfl) {
-            const int off = 1 << ((h.op >> kOpOffShift) & 7u);
-            shfl_step<T>(g, h, off, a, j, pb);
-            shfl_step<T>(g, h, off, b, j, pb);
-        } else {
-            diag_step<T>(g, h, a, j);
-            diag_step<T>(g, h, b, j);
+        switch (h.kind) {
+        case KX: gate_on<T, KX>(g, h, a, b, pb); break;
+        case KY: gate_on<T, KY>(g, h, a, b, pb); break;
+        case KZ: gate_on<T, KZ>(g, h, a, b, pb); break;
+        case KH: gate_on<T, KH>(g, h, a, b, pb); break;
+        case KPHASE: gate_on<T, KPHASE>(g, h, a, b, pb); break;
+        case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
+        case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
+        case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
+        case KS: gate_on<T, KS>(g, h, a, b, pb); break;
+        case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
+        case KT: gate_on<T, KT>(g, h, a, b, pb); break;
+        case KTDG: gate_on<T, KTDG>(g, h, a, b, pb); break;
+        case KU: gate_on<T, KU>(g, h, a, b, pb); break;
+        default: gate_on<T, KYPH>(g, h, a, b, pb); break;
         }
     }
 }
@@ -223,7 +242,7 @@ __device__ __forceinline__ long long write_val(const TableDev& t, unsigned ep, V
     long long fresh = -1;
     if (__any_sync(kFull, b < 0 && hm != 0)) {
         long long cb = -1;
-        if (b < 0 && hm && j == 0) cb = claim_group(t, ep, v.G, status, &created);
+        if (b < 0 && hm && j == 0) cb = claim_group(t, ep, v.key >> kSlotBits, status, &created);
         cb = (long long)shfl64((unsigned long long)cb, half << 4);
         created = __shfl_sync(kFull, (int)created, half << 4) != 0;
         if (b < 0 && hm) {
@@ -234,7 +253,7 @@ __device__ __forceinline__ long long write_val(const TableDev& t, unsigned ep, V
     if (b >= 0) {
         const size_t s = (size_t)b * kSlots + j;
         if (created || v.pres != v.pres0)
-            t.keys[s] = v.pres ? ((v.G << kSlotBits) | (unsigned long long)j) : empty_key(j);
+            t.keys[s] = v.pres ? v.key : empty_key(j);
         if (v.pres && v.dirty) store_amp<T>(t.amps, s, v.amp);
         cnt_nnz += v.pres ? 1 : 0;
         if (j == 0 && !hm) cnt_empty += 1;
@@ -262,7 +281,7 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 
 template <class T>
 __device__ __forceinline__ void load_val_g(const TableDev& t, Val<T>& v, unsigned long long G, long long b, int j) {
-    v.G = G;
+    v.key = (G << kSlotBits) | (unsigned long long)j;
     v.b = b;
     v.dirty = false;
     v.pres = false;
