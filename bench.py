@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-PROFILE_TXT = os.path.join(ROOT, "profiles", "pass_kernel_c2_fp64.txt")
+PROFILES = os.path.join(ROOT, "profiles")
 
 
 def parse_args():
@@ -155,18 +155,23 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the gate-pass kernel from the committed ncu summary, if any."""
+def read_profile(name):
+    """Key: value lines of a committed ncu summary (profiles/<name>.txt), {} if absent."""
+    out = {}
     try:
-        for line in open(PROFILE_TXT):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
+        for line in open(os.path.join(PROFILES, name + ".txt")):
+            if ":" in line and not line.startswith((" ", "#")):
+                k, v = line.split(":", 1)
+                try:
+                    out[k.strip()] = float(v.strip().split()[0])
+                except (ValueError, IndexError):
+                    pass
     except OSError:
         pass
-    return None
+    return out
 
 
-def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured, precision):
+def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured, precision, profile_name):
     """Roofline of the dominant gate-pass kernel over the timed steps.
 
     Every pass is bracketed by CUDA events on the engine's stream (time_passes); pair passes
@@ -181,16 +186,18 @@ def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured
     staged = s1["buckets"] > (1 << 20)
     T = "double" if precision == 64 else "float"
     kinds = {
-        "pair": {"kernel": (f"resolve_kernel + staged_kernel<{T}, true>" if staged else f"direct_kernel<{T}, true>"),
+        "pair": {"kernel": (f"resolve_kernel<1|2> + staged_kernel<{T}, 1|2>" if staged
+                            else f"direct_kernel<{T}, 1|2>") + " (passes pairing 16-key groups)",
                  "bytes": alg_pair_step * steps, "t": t_pair, "passes": n_pair},
-        "stream": {"kernel": f"staged_kernel<{T}, false>" if staged else f"direct_kernel<{T}, false>",
+        "stream": {"kernel": f"staged_kernel<{T}, 0>" if staged else f"direct_kernel<{T}, 0>",
                    "bytes": (alg_step - alg_pair_step) * steps, "t": t_stream, "passes": n_all - n_pair},
     }
     dom = max(kinds, key=lambda k: kinds[k]["t"])
     d = kinds[dom]
     achieved = d["bytes"] / d["t"] / 1e9 if d["t"] > 0 else 0.0
+    prof = read_profile(profile_name)
     out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-           "traffic": read_profile_traffic(), "kernel": d["kernel"],
+           "traffic": prof.get("traffic_bytes_per_launch"), "kernel": d["kernel"],
            "launches_per_step": d["passes"] * (2 if (staged and dom == "pair") else 1),
            "alg_bytes_per_pass": d["bytes"] / steps / max(d["passes"], 1),
            "avg_pass_us": 1e6 * d["t"] / steps / max(d["passes"], 1),
@@ -198,11 +205,27 @@ def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured
            "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs), of measured" if measured
                            else "fallback 6.8 TB/s, of fallback"),
            "whole_step_achieved": alg_step * steps / (dev_ms / 1e3) / 1e9}
+    if prof:
+        out["profile"] = f"profiles/{profile_name}.txt"
+        for k in ("fp64_pipe_active_pct", "issue_slots_used_pct", "dram_throughput_pct"):
+            if k in prof:
+                out[k + "_ncu"] = prof[k]
+        if precision == 64 and "fp64_pipe_active_pct" in prof:
+            out["note"] = ("FP64 gate arithmetic issues on the FP64 pipe (1/64 of the FP32 rate on this GPU); "
+                           "ncu's FP64-pipe activity for this kernel is the bound, not HBM")
     other = "stream" if dom == "pair" else "pair"
     o = kinds[other]
     out["other_kernel"] = {"kernel": o["kernel"], "achieved": o["bytes"] / o["t"] / 1e9 if o["t"] > 0 else 0.0,
                            "share_of_step_time": o["t"] * 1e3 / dev_ms if dev_ms > 0 else None}
     return out
+
+
+def profile_for(args, staged):
+    """Name of the committed ncu summary of this workload's dominant pass kernel."""
+    prec = f"fp{args.precision}"
+    if args.workload == "c4":
+        return f"batch_run_kernel_c4_{prec}"
+    return f"{'staged' if staged else 'direct'}_kernel_{args.workload}_{prec}"
 
 
 def measured_peaks():
@@ -334,7 +357,7 @@ def run_gpu(args):
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     roofline = pass_roofline(s0, s1, alg_per_step, alg_pair_step, args.steps, dev_ms, peak, peaks is not None,
-                             args.precision)
+                             args.precision, profile_for(args, s1["buckets"] > (1 << 20)))
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(gates, args.cpu_seconds, args.precision)

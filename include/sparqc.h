@@ -154,6 +154,27 @@ int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_
 /* Sum of |amplitude|^2, accumulated in FP64 on the device. */
 int sqc_norm2(sqc_state* st, double* norm2);
 
+/* ---- selection and measurement ---------------------------------------------------------- */
+/* Readout restricted to the keys with (key & mask) == value, as sqc_get_state (flags
+ * SQC_READ_SORTED sorts by key on the device). The reference's Circuit__::get_state_full
+ * selects states by a per-qubit pattern (state_to_choose: -1 any, 0, 1;
+ * emulator/include/circuit.h:206-253): its qubits fixed to 0 or 1 are the mask bits, their
+ * values the value bits. */
+int sqc_get_state_where(sqc_state* st, uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im,
+                        uint64_t cap, uint64_t* n, uint32_t flags);
+/* Sum of |amplitude|^2 over the keys with (key & mask) == value (FP64, on the device). */
+int sqc_probability(sqc_state* st, uint64_t mask, uint64_t value, double* p);
+/* Projective measurement of one qubit (no counterpart in the reference): outcome 1 iff
+ * u < p1, p1 = probability of reading 1 divided by the norm; the keys of the other outcome are
+ * removed and the remaining amplitudes multiplied by 1/sqrt(their total probability).
+ * u must be in [0, 1); *p1 (may be NULL) receives p1. */
+int sqc_measure(sqc_state* st, uint32_t qubit, double u, int* outcome, double* p1);
+/* shots basis states drawn with probability |amplitude|^2 / norm (no counterpart in the
+ * reference): the keys are sorted, their probabilities summed into a cumulative distribution,
+ * and shot s takes the first key whose cumulative probability exceeds u_s * total, with u_s a
+ * splitmix64 hash of (seed, s). The same state and seed give the same samples. */
+int sqc_sample(sqc_state* st, uint64_t shots, uint64_t seed, uint64_t* keys);
+
 /* Compare two states of equal qubit count on the device (FP64 accumulation):
  * fidelity = |<b|a>|^2 / (<a|a><b|b>), max_abs_err = max over keys of |a_k - b_k|. */
 int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_err);

@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <initializer_list>
+#include <map>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -120,6 +121,44 @@ public:
         vv_.reserve(k.size());
         for (size_t n = 0; n < k.size(); ++n) vv_[k[n]] = TComplex{r[n], i[n]};
         return vv_;
+    }
+
+    /* Key-ordered non-negligible entries matching a per-qubit pattern, as get_state_full selects
+     * them (emulator/include/circuit.h:206-253): state_to_choose[q] is -1 (any), 0 or 1; an
+     * empty pattern selects everything. The selection and the ordering run on the GPU. */
+    std::map<uint64_t, TComplex> get_state_full(const std::vector<short>& state_to_choose = {}) {
+        uint64_t mask = 0, value = 0;
+        for (size_t q = 0; q < state_to_choose.size() && q < 64; ++q) {
+            if (state_to_choose[q] < 0) continue;
+            mask |= uint64_t(1) << q;
+            if (state_to_choose[q]) value |= uint64_t(1) << q;
+        }
+        uint64_t n = nnz();
+        std::vector<uint64_t> k(n);
+        std::vector<double> r(n), i(n);
+        check(sqc_get_state_where(st_, mask, value, k.data(), r.data(), i.data(), n, &n,
+                                  SQC_READ_SORTED | SQC_READ_DROP_NEGLIGIBLE),
+              "get_state_full");
+        std::map<uint64_t, TComplex> out;
+        for (uint64_t m = 0; m < n; ++m) out.emplace_hint(out.end(), k[m], TComplex{r[m], i[m]});
+        return out;
+    }
+
+    /* additions: probability of a pattern, measurement of one qubit with collapse, sampling */
+    double probability(uint64_t mask, uint64_t value) {
+        double p = 0.0;
+        check(sqc_probability(st_, mask, value, &p), "probability");
+        return p;
+    }
+    int measure(uint32_t q, double u, double* p1 = nullptr) {
+        int out = 0;
+        check(sqc_measure(st_, q, u, &out, p1), "measure");
+        return out;
+    }
+    std::vector<uint64_t> sample(uint64_t shots, uint64_t seed = 0) {
+        std::vector<uint64_t> k(shots);
+        check(sqc_sample(st_, shots, seed, k.data()), "sample");
+        return k;
     }
 
     /* prints "key: re + imj" per nonzero, as print_raw_data does (emulator/include/circuit.h:88-92) */

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsparqc.so")
-SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_batch.cu", "sqc_engine.cpp", "sqc_plan.cpp", "sqc_batch.cpp",
+SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_batch.cu", "sqc_measure.cu", "sqc_engine.cpp", "sqc_plan.cpp", "sqc_batch.cpp",
            "sqc_serve.cpp",
            "sqc_capi.cpp", "sqc_capi_batch.cpp", "sqc_fixed.cu"]
 # per-file extra flags: the persistent batch kernel reads data other SMs wrote during the

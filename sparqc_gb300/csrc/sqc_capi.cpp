@@ -122,6 +122,23 @@ int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_er
     return guarded(a, [&](sqc::Engine& e) { return e.compare(b->eng, fidelity, max_abs_err); });
 }
 
+int sqc_get_state_where(sqc_state* st, uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im,
+                        uint64_t cap, uint64_t* n, uint32_t flags) {
+    return guarded(st, [&](sqc::Engine& e) { return e.get_state_where(mask, value, keys, re, im, cap, n, flags); });
+}
+
+int sqc_probability(sqc_state* st, uint64_t mask, uint64_t value, double* p) {
+    return guarded(st, [&](sqc::Engine& e) { return e.probability(mask, value, p); });
+}
+
+int sqc_measure(sqc_state* st, uint32_t qubit, double u, int* outcome, double* p1) {
+    return guarded(st, [&](sqc::Engine& e) { return e.measure(qubit, u, outcome, p1); });
+}
+
+int sqc_sample(sqc_state* st, uint64_t shots, uint64_t seed, uint64_t* keys) {
+    return guarded(st, [&](sqc::Engine& e) { return e.sample(shots, seed, keys); });
+}
+
 int sqc_get_stats(sqc_state* st, sqc_stats* out) {
     if (!out) return SQC_ERR_ARG;
     return guarded(st, [&](sqc::Engine& e) { return e.stats(out); });

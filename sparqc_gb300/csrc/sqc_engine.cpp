@@ -37,6 +37,9 @@ Engine::~Engine() {
     if (d_rk_) cudaFree(d_rk_);
     if (d_rr_) cudaFree(d_rr_);
     if (d_ri_) cudaFree(d_ri_);
+    for (void* p : {(void*)sort_.keys_out, (void*)sort_.re_out, (void*)sort_.im_out, (void*)sort_.idx_in,
+                    (void*)sort_.idx_out, (void*)sort_.cum, sort_.tmp})
+        if (p) cudaFree(p);
     for (cudaEvent_t e : ev_all_) cudaEventDestroy(e);
     if (own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
@@ -515,41 +518,145 @@ int Engine::nnz(uint64_t* out) {
     return SQC_OK;
 }
 
-int Engine::get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
+int Engine::ensure_sort(size_t n) {
+    if (n <= sort_cap_) return SQC_OK;
+    const size_t cap = std::max<size_t>(n, 1024);
+    for (void* p : {(void*)sort_.keys_out, (void*)sort_.re_out, (void*)sort_.im_out, (void*)sort_.idx_in,
+                    (void*)sort_.idx_out, (void*)sort_.cum, sort_.tmp})
+        if (p) cudaFree(p);
+    sort_ = SortBuffers();
+    sort_cap_ = 0;
+    const size_t tmp = sort_scratch_bytes(cap);
+    int rc;
+    if ((rc = cuda(cudaMalloc(&sort_.keys_out, cap * 8), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.re_out, cap * 8), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.im_out, cap * 8), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.idx_in, cap * 4), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.idx_out, cap * 4), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.cum, cap * 8), "cudaMalloc(sort)")) ||
+        (rc = cuda(cudaMalloc(&sort_.tmp, tmp), "cudaMalloc(sort)")))
+        return rc;
+    sort_.tmp_bytes = tmp;
+    sort_cap_ = cap;
+    return SQC_OK;
+}
+
+// Compact the present keys with (actual & mask) == value into the device readout arrays
+// (actual keys); *got receives their number (also when it exceeds the arrays).
+int Engine::readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got) {
     int rc = sync();
     if (rc) return rc;
-    const unsigned long long have = ctl_host_->nnz;
-    if ((rc = ensure_readout(have))) return rc;
+    if ((rc = ensure_readout(ctl_host_->nnz))) return rc;
     if ((rc = cuda(cudaMemsetAsync(&ctl_->out_count, 0, sizeof(unsigned long long), stream_), "memset"))) return rc;
-    if ((rc = cuda(launch_readout(dev(), ctl_, list_hint_, plan_.frame, dbl_, d_rk_, d_rr_, d_ri_, rcap_,
-                                  (flags & SQC_READ_DROP_NEGLIGIBLE) != 0, prune_, sms_, stream_),
+    if ((rc = cuda(launch_readout(dev(), ctl_, list_hint_, plan_.frame, dbl_, d_rk_, d_rr_, d_ri_, rcap_, drop_negl,
+                                  prune_, sms_, stream_, mask, value ^ (plan_.frame & mask)),
                    "readout")))
         return rc;
     ++launches_;
     if ((rc = read_ctl())) return rc;
-    const unsigned long long got = ctl_host_->out_count;
+    *got = ctl_host_->out_count;
+    return SQC_OK;
+}
+
+int Engine::get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
+    return get_state_where(0, 0, keys, re, im, cap, n, flags);
+}
+
+int Engine::get_state_where(uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im, uint64_t cap,
+                            uint64_t* n, uint32_t flags) {
+    unsigned long long got = 0;
+    int rc = readout_to_device(mask, value, (flags & SQC_READ_DROP_NEGLIGIBLE) != 0, &got);
+    if (rc) return rc;
     if (n) *n = got;
     if (got > cap) return fail(SQC_ERR_CAPACITY, "output arrays too small");
     if (got && (!keys || !re || !im)) return fail(SQC_ERR_ARG, "null output array");
-    if (got) {
-        if ((rc = cuda(cudaMemcpyAsync(keys, d_rk_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H keys")) ||
-            (rc = cuda(cudaMemcpyAsync(re, d_rr_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H re")) ||
-            (rc = cuda(cudaMemcpyAsync(im, d_ri_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H im")) ||
-            (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
-            return rc;
+    if (!got) return SQC_OK;
+    const unsigned long long* sk = d_rk_;
+    const double* sr = d_rr_;
+    const double* si = d_ri_;
+    if ((flags & SQC_READ_SORTED) && got > 1) {   // key sort on the device
+        if ((rc = ensure_sort(got))) return rc;
+        sort_.keys_in = d_rk_;
+        sort_.re_in = d_rr_;
+        sort_.im_in = d_ri_;
+        if ((rc = cuda(sort_entries(sort_, got, nq_, false, sms_, stream_), "sort"))) return rc;
+        launches_ += 3;
+        sk = sort_.keys_out;
+        sr = sort_.re_out;
+        si = sort_.im_out;
     }
-    if ((flags & SQC_READ_SORTED) && got > 1) {
-        std::vector<uint64_t> idx(got);
-        std::iota(idx.begin(), idx.end(), 0);
-        std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) { return keys[a] < keys[b]; });
-        std::vector<uint64_t> k2(got);
-        std::vector<double> r2(got), i2(got);
-        for (uint64_t i = 0; i < got; ++i) { k2[i] = keys[idx[i]]; r2[i] = re[idx[i]]; i2[i] = im[idx[i]]; }
-        std::memcpy(keys, k2.data(), got * 8);
-        std::memcpy(re, r2.data(), got * 8);
-        std::memcpy(im, i2.data(), got * 8);
-    }
+    if ((rc = cuda(cudaMemcpyAsync(keys, sk, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H keys")) ||
+        (rc = cuda(cudaMemcpyAsync(re, sr, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H re")) ||
+        (rc = cuda(cudaMemcpyAsync(im, si, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H im")) ||
+        (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
+        return rc;
     return SQC_OK;
+}
+
+int Engine::probability(uint64_t mask, uint64_t value, double* p) {
+    if (!p) return fail(SQC_ERR_ARG, "null output");
+    int rc = sync();
+    if (rc) return rc;
+    if ((rc = cuda(cudaMemsetAsync(&ctl_->acc[0], 0, sizeof(double), stream_), "memset")) ||
+        (rc = cuda(launch_pattern_prob(dev(), ctl_, list_hint_, dbl_, mask, value ^ (plan_.frame & mask), sms_,
+                                       stream_),
+                   "probability")))
+        return rc;
+    ++launches_;
+    if ((rc = read_ctl())) return rc;
+    *p = ctl_host_->acc[0];
+    return SQC_OK;
+}
+
+// Projective measurement of one qubit: outcome 1 iff u < p1 / norm, then the keys of the other
+// outcome are removed and the rest renormalised; the measured bit becomes known to the planner.
+int Engine::measure(uint32_t qubit, double u, int* outcome, double* p1) {
+    if (qubit >= nq_) return fail(SQC_ERR_ARG, "qubit out of range");
+    if (!(u >= 0.0 && u < 1.0)) return fail(SQC_ERR_ARG, "u must be in [0, 1)");
+    double norm = 0.0, one = 0.0;
+    int rc;
+    if ((rc = norm2(&norm)) || (rc = probability(1ULL << qubit, 1ULL << qubit, &one))) return rc;
+    if (!(norm > 0.0)) return fail(SQC_ERR_STATE, "measurement of an empty state");
+    const double prob1 = one / norm;
+    const int out = u < prob1 ? 1 : 0;
+    const double kept = out ? one : norm - one;
+    if (!(kept > 0.0)) return fail(SQC_ERR_STATE, "measurement outcome of probability zero");
+    const unsigned long long bit = 1ULL << qubit;
+    const unsigned long long val = out ? bit : 0ULL;
+    if ((rc = cuda(launch_collapse(dev(), ctl_, list_hint_, dbl_, bit, val ^ (plan_.frame & bit), 1.0 / std::sqrt(kept),
+                                   sms_, stream_),
+                   "collapse")))
+        return rc;
+    launches_ += 2;
+    if ((rc = read_ctl())) return rc;
+    plan_.kmask |= bit;
+    plan_.kval = (plan_.kval & ~bit) | val;
+    snap_plan_ = plan_;
+    if (outcome) *outcome = out;
+    if (p1) *p1 = prob1;
+    return SQC_OK;
+}
+
+int Engine::sample(uint64_t shots, uint64_t seed, uint64_t* keys) {
+    if (shots && !keys) return fail(SQC_ERR_ARG, "null output array");
+    unsigned long long got = 0;
+    int rc = readout_to_device(0, 0, false, &got);
+    if (rc) return rc;
+    if (!shots) return SQC_OK;
+    if (!got) return fail(SQC_ERR_STATE, "sampling an empty state");
+    if ((rc = ensure_sort(got))) return rc;
+    sort_.keys_in = d_rk_;
+    sort_.re_in = d_rr_;
+    sort_.im_in = d_ri_;
+    if ((rc = cuda(sort_entries(sort_, got, nq_, true, sms_, stream_), "sort"))) return rc;
+    unsigned long long* d_out = nullptr;
+    if ((rc = cuda(cudaMallocAsync(&d_out, shots * 8, stream_), "cudaMallocAsync(samples)"))) return rc;
+    rc = cuda(launch_sample(sort_.keys_out, sort_.cum, got, seed, shots, d_out, sms_, stream_), "sample");
+    if (!rc) rc = cuda(cudaMemcpyAsync(keys, d_out, shots * 8, cudaMemcpyDeviceToHost, stream_), "D2H samples");
+    cudaFreeAsync(d_out, stream_);
+    if (!rc) rc = cuda(cudaStreamSynchronize(stream_), "sync");
+    launches_ += 5;
+    return rc;
 }
 
 int Engine::norm2(double* out) {

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sparqc.h"
+#include "sqc_measure.h"
 #include "sqc_plan.h"
 #include "sqc_types.h"
 
@@ -44,6 +45,12 @@ public:
     int sync();
     int nnz(uint64_t* out);
     int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
+    // Readout of the keys with (key & mask) == value (actual keys, not the stored frame).
+    int get_state_where(uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im, uint64_t cap,
+                        uint64_t* n, uint32_t flags);
+    int probability(uint64_t mask, uint64_t value, double* p);
+    int measure(uint32_t qubit, double u, int* outcome, double* p1);
+    int sample(uint64_t shots, uint64_t seed, uint64_t* keys);
     int norm2(double* out);
     int compare(Engine& b, double* fidelity, double* max_abs_err);
     // Compare this state (a) with a table that another object owns (b, on the same device,
@@ -68,6 +75,8 @@ private:
     int repair(size_t failed_pass);
     int ensure_desc(size_t n);
     int ensure_readout(size_t n);
+    int ensure_sort(size_t n);
+    int readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got);
     bool plan_gate(const sqc_gate& g, GateDesc* out);
     int read_ctl();
     int record_event(cudaEvent_t* out);
@@ -110,6 +119,8 @@ private:
     double* d_rr_ = nullptr;
     double* d_ri_ = nullptr;
     size_t rcap_ = 0;
+    SortBuffers sort_;            // device key sort of readouts (sorted readout, sampling)
+    size_t sort_cap_ = 0;
 
     uint64_t gates_applied_ = 0, passes_run_ = 0, launches_ = 0, replays_ = 0, rebuilds_ = 0;
     uint64_t passes_pair_ = 0;

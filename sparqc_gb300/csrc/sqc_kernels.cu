@@ -52,6 +52,7 @@ __global__ void set_zero_kernel(TableDev t, Ctl* ctl, int dbl) {
         ctl->epoch += 1;
         ctl->status = 0;
         ctl->done = 0;
+        ctl->work = 0;
         ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
         ctl->seq = 0;
         ctl->amp_updates = 0;
@@ -84,6 +85,7 @@ __global__ void set_state_begin_kernel(Ctl* ctl) {
     ctl->epoch += 1;
     ctl->status = 0;
     ctl->done = 0;
+    ctl->work = 0;
     ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
     ctl->seq = 0;
     ctl->amp_updates = 0;
@@ -164,13 +166,14 @@ __global__ void count_kernel(TableDev t, Ctl* ctl) {
     }
 }
 
-// Compact the present entries into (keys ^ frame, re, im). Each warp owns a contiguous range
-// of list entries: it counts, reserves its span with one atomic, then writes. Entries beyond
-// cap are counted but not written.
+// Compact the present entries whose stored key matches (key & smask) == sval into
+// (keys ^ frame, re, im). Each warp owns a contiguous range of list entries: it counts,
+// reserves its span with one atomic, then writes. Entries beyond cap are counted but not
+// written.
 template <class T>
 __global__ void readout_kernel(TableDev t, Ctl* ctl, unsigned long long frame, unsigned long long* okeys,
                                double* ore, double* oim, unsigned long long cap, int drop_negl, PruneBits pb,
-                               unsigned long long range) {
+                               unsigned long long range, unsigned long long smask, unsigned long long sval) {
     const unsigned long long n = ctl->list_n;
     const int lane = threadIdx.x & 31, j = lane & 15, half = lane >> 4;
     const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -183,7 +186,8 @@ __global__ void readout_kernel(TableDev t, Ctl* ctl, unsigned long long frame, u
             bool keep = false;
             if (e < r1) {
                 const size_t s = (size_t)t.list[e] * kSlots + j;
-                keep = slot_present(t.keys[s], j);
+                const unsigned long long k = t.keys[s];
+                keep = slot_present(k, j) && (k & smask) == sval;
                 if (keep && drop_negl) keep = !negligible(load_amp<T>(t.amps, s), pb);
             }
             cnt += __popc(__ballot_sync(kFull, keep));
@@ -199,7 +203,8 @@ __global__ void readout_kernel(TableDev t, Ctl* ctl, unsigned long long frame, u
             size_t s = 0;
             if (e < r1) {
                 s = (size_t)t.list[e] * kSlots + j;
-                keep = slot_present(t.keys[s], j);
+                const unsigned long long k = t.keys[s];
+                keep = slot_present(k, j) && (k & smask) == sval;
                 if (keep && drop_negl) keep = !negligible(load_amp<T>(t.amps, s), pb);
             }
             const unsigned bal = __ballot_sync(kFull, keep);
@@ -383,11 +388,16 @@ cudaError_t launch_count(const TableDev& t, Ctl* ctl, unsigned long long list_hi
 
 cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_hint, unsigned long long frame,
                            bool dbl, unsigned long long* okeys, double* ore, double* oim, unsigned long long cap,
-                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st) {
+                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st, unsigned long long smask,
+                           unsigned long long sval) {
     const unsigned long long range = 64;
     const int grid = grid_for((list_hint + range - 1) / range + 1, kThreads / 32, sms);
-    if (dbl) readout_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range);
-    else readout_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range);
+    if (dbl)
+        readout_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range,
+                                                           smask, sval);
+    else
+        readout_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, frame, okeys, ore, oim, cap, drop_negl, pb, range,
+                                                          smask, sval);
     return cudaGetLastError();
 }
 

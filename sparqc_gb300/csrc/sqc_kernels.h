@@ -20,9 +20,11 @@ cudaError_t launch_set_state(const unsigned long long* keys, const double* re, c
                              unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,
                              cudaStream_t st);
 cudaError_t launch_count(const TableDev& t, Ctl* ctl, unsigned long long list_hint, int sms, cudaStream_t st);
+// Readout of the present entries whose stored key k has (k & smask) == sval (all by default).
 cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_hint, unsigned long long frame,
                            bool dbl, unsigned long long* okeys, double* ore, double* oim, unsigned long long cap,
-                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st);
+                           bool drop_negl, PruneBits pb, int sms, cudaStream_t st, unsigned long long smask = 0,
+                           unsigned long long sval = 0);
 cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, int sms,
                         cudaStream_t st);
 cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,

@@ -69,6 +69,7 @@ __device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e
             ctl->seq += 1;
         }
         ctl->done = 0;
+        ctl->work = 0;
         __threadfence();
     }
 }
@@ -97,12 +98,17 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
     const unsigned long long nnz_in = ctl->nnz;
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
-    const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
     Val<T> va, vb;
+    // warps take four list entries at a time from the pass's work counter, so they finish
+    // together whatever the number of units each group of entries owns
+    auto next4 = [&]() -> unsigned long long {
+        unsigned long long e = 0;
+        if (lane == 0) e = atomicAdd(&ctl->work, 4ULL);
+        return shfl64(e, 0);
+    };
     if (NX == 0) {
-        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+        for (unsigned long long e0 = next4(); e0 < n; e0 = next4()) {
             const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
             const long long ba = ea < n ? (long long)t.list[ea] : -1;
             const long long bb = eb < n ? (long long)t.list[eb] : -1;
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
     } else {
         const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
         const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
-        for (unsigned long long e0 = warp * 4; e0 < n; e0 += nwarps * 4) {
+        for (unsigned long long e0 = next4(); e0 < n; e0 = next4()) {
             long long mb;
             unsigned long long G0;
             const unsigned om = units4<NX>(t, ep, e0, n, m1, m2, lane, &mb, &G0);
@@ -211,11 +217,20 @@ __device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsi
 
 // Where a warp's next slot comes from: a strided sequence of 4-entry items (stream pass) or
 // the dense owned pairs of a strided sequence of ranges (pair pass).
+// Items (four list entries, stream passes) and ranges (pair and quad passes) are handed out
+// from the pass's work counter, so the warps finish together.
 struct SlotSource {
-    unsigned long long next;      // stream: next item; pair: current range
-    unsigned long long u, c;      // pair: next unit within the range, units in the range
-    unsigned long long stride, end;
+    unsigned long long next;      // stream: current item; pair/quad: current range
+    unsigned long long u, c;      // pair/quad: next unit within the range, units in the range
+    unsigned long long end;
+    Ctl* ctl;
 };
+
+__device__ __forceinline__ unsigned long long grab_work(Ctl* ctl, int lane) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(&ctl->work, 1ULL);
+    return shfl64(w, 0);
+}
 
 template <class T, int NX>
 __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotSource& src, unsigned long long n,
@@ -228,15 +243,15 @@ __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotS
     unsigned long long Gk = 0;
     bool any = false;
     if (NX == 0) {
+        if (src.next < src.end) src.next = grab_work(src.ctl, lane);
         if (src.next < src.end) {
             const unsigned long long e = 4 * src.next + (unsigned long long)lane;
             if (lane < 4 && e < n) bk = t.list[e];
-            src.next += src.stride;
             any = true;
         }
     } else {
         while (src.next < src.end && src.u >= src.c) {   // move to the next range with units
-            src.next += src.stride;
+            src.next = grab_work(src.ctl, lane);
             src.u = 0;
             src.c = src.next < src.end ? t.counts[src.next] : 0;
         }
@@ -310,22 +325,15 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
     const unsigned long long nnz_in = ctl->nnz;
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, jj = lane & 15;
-    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     const unsigned long long R = a.range;
     const unsigned long long m1 = NX ? 1ULL << (a.q1 - kSlotBits) : 0ULL;
     const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
     SlotSource src;
-    src.next = gw;
-    src.stride = nw;
+    src.ctl = ctl;
+    src.next = 0;
     src.u = 0;
-    if (NX == 0) {
-        src.end = (n + 3) / 4;
-        src.c = 0;
-    } else {
-        src.end = (n + R - 1) / R;
-        src.c = src.next < src.end ? t.counts[src.next] : 0;
-    }
+    src.c = 0;
+    src.end = NX == 0 ? (n + 3) / 4 : (n + R - 1) / R;
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
     for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, R, m1, m2, lane);
     Val<T> va, vb;

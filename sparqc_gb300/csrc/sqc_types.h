@@ -68,6 +68,7 @@ struct Ctl {
     unsigned long long out_count;   // readout counter
     double acc[6];                  // reductions: norm, compare
     unsigned long long acc_max;     // bit pattern of a non-negative double (max |a-b|)
+    unsigned long long work;        // list entries handed out in the running pass (0 between passes)
 };
 
 // Gate descriptor with host-resolved coefficients (std::cos/std::sin on the host, so the

@@ -22,6 +22,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_apply_gates", "sqc_x", "sqc_y", "sqc_z", "sqc_h", "sqc_phase", "sqc_rz", "sqc_rx", "sqc_ry",
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
+           "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_autotune", "sqc_batch_get_stats", "sqc_batch_compare", "sqc_batch_last_error",
@@ -128,6 +129,12 @@ def load(path=LIB_PATH):
     L.sqc_norm2.argtypes = [P, ctypes.POINTER(D)]
     L.sqc_compare.argtypes = [P, P, ctypes.POINTER(D), ctypes.POINTER(D)]
     L.sqc_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+    L.sqc_get_state_where.argtypes = [P, U64, U64, P, P, P, U64, ctypes.POINTER(U64), U32]
+    L.sqc_probability.argtypes = [P, U64, U64, ctypes.POINTER(D)]
+    L.sqc_measure.argtypes = [P, U32, D, ctypes.POINTER(I), ctypes.POINTER(D)]
+    L.sqc_sample.argtypes = [P, U64, U64, P]
+    for n in ("sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample"):
+        getattr(L, n).restype = I
     L.sqc_status_string.argtypes = [I]
     L.sqc_status_string.restype = ctypes.c_char_p
     L.sqc_last_error.argtypes = [P]
@@ -280,6 +287,35 @@ class State:
                     "get_state")
         m = got.value
         return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def state_where(self, mask, value, sorted=True, drop_negligible=False):
+        """Entries whose keys have (key & mask) == value."""
+        n = self.nnz
+        keys = np.empty(max(n, 1), np.uint64)
+        re = np.empty(max(n, 1), np.float64)
+        im = np.empty(max(n, 1), np.float64)
+        got = ctypes.c_uint64()
+        flags = (READ_SORTED if sorted else 0) | (READ_DROP_NEGLIGIBLE if drop_negligible else 0)
+        self._check(self._L.sqc_get_state_where(self._h, mask, value, _p(keys), _p(re), _p(im), n,
+                                                ctypes.byref(got), flags), "get_state_where")
+        m = got.value
+        return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def probability(self, mask, value):
+        p = ctypes.c_double()
+        self._check(self._L.sqc_probability(self._h, mask, value, ctypes.byref(p)), "probability")
+        return p.value
+
+    def measure(self, qubit, u):
+        """Measure one qubit with the uniform number u in [0, 1): (outcome, probability of 1)."""
+        o, p1 = ctypes.c_int(), ctypes.c_double()
+        self._check(self._L.sqc_measure(self._h, qubit, u, ctypes.byref(o), ctypes.byref(p1)), "measure")
+        return o.value, p1.value
+
+    def sample(self, shots, seed=0):
+        out = np.empty(max(shots, 1), np.uint64)
+        self._check(self._L.sqc_sample(self._h, shots, seed, _p(out)), "sample")
+        return out[:shots]
 
     def norm2(self):
         v = ctypes.c_double()

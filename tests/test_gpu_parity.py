@@ -261,6 +261,16 @@ int main() {
         for (uint32_t ii = 0; ii < nq; ii++) oc.h(ii);
         oc.rx(3, 0.5); oc.phase(7, 0.25); oc.controlled(SQC_X, 30 % nq, {1, 2});
         std::printf("nnz %llu norm %.15f\n", (unsigned long long)oc.nnz(), oc.norm2());
+        std::vector<short> pattern(nq, -1);
+        pattern[0] = 1; pattern[5] = 0;
+        auto sel = oc.get_state_full(pattern);
+        bool ordered = true, match = true;
+        uint64_t prev = 0;
+        for (auto& kv : sel) { ordered = ordered && (kv.first >= prev); prev = kv.first;
+                               match = match && (kv.first & 1) && !((kv.first >> 5) & 1); }
+        std::printf("selected %zu ordered %d match %d\n", sel.size(), (int)ordered, (int)match);
+        int m = oc.measure(0, 0.25);
+        std::printf("measured %d nnz %llu samples %zu\n", m, (unsigned long long)oc.nnz(), oc.sample(10, 3).size());
         try { Circuit__ bad(8, [] { hash_table_parameters p; p.N_devices = 2; return p; }()); }
         catch (const std::string& e) { std::printf("caught: %s\n", e.c_str()); }
     } catch (const std::string& e) { std::printf("error: %s\n", e.c_str()); return 1; }
@@ -273,3 +283,4 @@ int main() {
                     "-L", lib, "-lsparqc", f"-Wl,-rpath,{lib}"], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
     assert "nnz 16777216" in out and "norm 1.0000000" in out and "caught:" in out
+    assert "selected 4194304 ordered 1 match 1" in out and "nnz 8388608 samples 10" in out
