@@ -197,7 +197,8 @@ def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured
     achieved = d["bytes"] / d["t"] / 1e9 if d["t"] > 0 else 0.0
     prof = read_profile(profile_name)
     out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-           "traffic": prof.get("traffic_bytes_per_launch"), "kernel": d["kernel"],
+           "traffic": (prof["traffic_bytes_per_launch"] * prof.get("traffic_scale", 1.0)
+                       if "traffic_bytes_per_launch" in prof else None), "kernel": d["kernel"],
            "launches_per_step": d["passes"] * (2 if (staged and dom == "pair") else 1),
            "alg_bytes_per_pass": d["bytes"] / steps / max(d["passes"], 1),
            "avg_pass_us": 1e6 * d["t"] / steps / max(d["passes"], 1),

@@ -120,6 +120,10 @@ int sqc_set_state(sqc_state* st, const uint64_t* keys, const double* re, const d
 /* Queue n gates (host array). Asynchronous. Replaces TableManager__::gate_sq/gate_sq_par. */
 int sqc_apply_gates(sqc_state* st, const sqc_gate* gates, uint64_t n);
 
+/* SWAP of qubits a and b (no counterpart in the reference): queued as the three CNOTs
+ * CX(a->b) CX(b->a) CX(a->b), each a controlled X, so it is exact. */
+int sqc_swap(sqc_state* st, uint32_t a, uint32_t b);
+
 /* One-gate conveniences with the reference's names (emulator/include/circuit.h:45-83),
  * uncontrolled. */
 int sqc_x(sqc_state* st, uint32_t t);
@@ -153,6 +157,15 @@ int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_
 
 /* Sum of |amplitude|^2, accumulated in FP64 on the device. */
 int sqc_norm2(sqc_state* st, double* norm2);
+
+/* ---- snapshots ------------------------------------------------------------------------ */
+/* Write the state to a file / replace the state with a file's (no counterpart in the
+ * reference, which names _RESTART.hdf5 files, emulator/include/QLib.h:39-40, but never writes
+ * them). Plain binary, little endian: the 8 bytes "SQCSNAP1", uint32 nq, uint32 precision,
+ * uint64 n, then n uint64 keys sorted ascending, n double re, n double im. Loading needs the
+ * same qubit count; amplitudes are rounded to the state's precision. */
+int sqc_save(sqc_state* st, const char* path);
+int sqc_load(sqc_state* st, const char* path);
 
 /* ---- selection and measurement ---------------------------------------------------------- */
 /* Readout restricted to the keys with (key & mask) == value, as sqc_get_state (flags

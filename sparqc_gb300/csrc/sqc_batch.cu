@@ -66,7 +66,7 @@ __device__ __forceinline__ void stream_chunk(const TableDev& t, const GateDesc* 
         const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
         load_val_g<T>(t, va, Ga, ba, j);
         load_val_g<T>(t, vb, Gb, bb, j);
-        run_gates<T>(gates, g0, g1, va, vb, lane, pb, upd);
+        run_gates<T, false>(gates, g0, g1, va, vb, lane, pb, upd);
         write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
     }
@@ -87,7 +87,8 @@ __device__ __forceinline__ void unit_chunk(const TableDev& t, const GateDesc* ga
         long long mb;
         unsigned long long G0;
         const unsigned om = units4<NX>(t, ep, e0, ee, m1, m2, lane, &mb, &G0);
-        run_units4<T, NX>(t, ep, ctl, gates, g0, g1, m1, m2, om, mb, G0, lane, pb, va, vb, cnt_nnz, cnt_empty, upd);
+        run_units4<T, NX, false>(t, ep, ctl, gates, g0, g1, m1, m2, om, mb, G0, lane, pb, va, vb, cnt_nnz, cnt_empty,
+                                 upd);
     }
 }
 

@@ -122,6 +122,32 @@ int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_er
     return guarded(a, [&](sqc::Engine& e) { return e.compare(b->eng, fidelity, max_abs_err); });
 }
 
+int sqc_swap(sqc_state* st, uint32_t a, uint32_t b) {
+    if (a == b) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) -> int {
+        sqc_gate g[3];
+        const uint32_t tgt[3] = {b, a, b}, ctl[3] = {a, b, a};
+        for (int i = 0; i < 3; ++i) {
+            g[i].kind = SQC_X;
+            g[i].target = tgt[i];
+            g[i].controls = 1ULL << (ctl[i] & 63);
+            g[i].theta = g[i].phi = g[i].lambda = 0.0;
+        }
+        if (a >= e.nq() || b >= e.nq()) return (int)SQC_ERR_ARG;
+        return e.apply(g, 3);
+    });
+}
+
+int sqc_save(sqc_state* st, const char* path) {
+    if (!path) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) { return e.save(path); });
+}
+
+int sqc_load(sqc_state* st, const char* path) {
+    if (!path) return SQC_ERR_ARG;
+    return guarded(st, [&](sqc::Engine& e) { return e.load(path); });
+}
+
 int sqc_get_state_where(sqc_state* st, uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im,
                         uint64_t cap, uint64_t* n, uint32_t flags) {
     return guarded(st, [&](sqc::Engine& e) { return e.get_state_where(mask, value, keys, re, im, cap, n, flags); });

@@ -233,6 +233,37 @@ __device__ __forceinline__ Cx<T> swap_update(bool bit, Cx<T> b) {
     else return bit ? Cx<T>{neg(b.i), b.r} : Cx<T>{b.i, neg(b.r)};   // Y
 }
 
+// Kind parameter of the update templates meaning "the kind is only known at run time".
+constexpr uint32_t KANY = 0xFFu;
+
+// Run-time dispatch of the updates (one copy of each kind's code per call site).
+template <class T>
+__device__ __forceinline__ Cx<T> branch_update_rt(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
+    switch (kind) {
+    case KH: return branch_update<T, KH>(g, bit, a, b);
+    case KRX: return branch_update<T, KRX>(g, bit, a, b);
+    case KRY: return branch_update<T, KRY>(g, bit, a, b);
+    default: return branch_update<T, KU>(g, bit, a, b);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ Cx<T> diag_update_rt(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a) {
+    switch (kind) {
+    case KZ: return diag_update<T, KZ>(g, bit, a);
+    case KS: return diag_update<T, KS>(g, bit, a);
+    case KSDG: return diag_update<T, KSDG>(g, bit, a);
+    case KYPH: return diag_update<T, KYPH>(g, bit, a);
+    case KRZ: return diag_update<T, KRZ>(g, bit, a);
+    default: return diag_update<T, KPHASE>(g, bit, a);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ Cx<T> swap_update_rt(uint32_t kind, bool bit, Cx<T> b) {
+    return kind == KX ? swap_update<T, KX>(bit, b) : swap_update<T, KY>(bit, b);
+}
+
 __host__ __device__ constexpr bool branch_kind(uint32_t k) { return k == KH || k == KRX || k == KRY || k == KU; }
 __host__ __device__ constexpr bool swap_kind(uint32_t k) { return k == KX || k == KY; }
 __host__ __device__ constexpr bool one_sided_kind(uint32_t k) {

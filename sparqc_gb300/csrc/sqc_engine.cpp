@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 
@@ -591,6 +592,50 @@ int Engine::get_state_where(uint64_t mask, uint64_t value, uint64_t* keys, doubl
         (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
         return rc;
     return SQC_OK;
+}
+
+// Snapshot file: "SQCSNAP1", uint32 nq, uint32 precision, uint64 n, keys (sorted), re, im.
+int Engine::save(const char* path) {
+    uint64_t n = 0;
+    int rc = nnz(&n);
+    if (rc) return rc;
+    std::vector<uint64_t> k(n);
+    std::vector<double> r(n), i(n);
+    if ((rc = get_state(k.data(), r.data(), i.data(), n, &n, SQC_READ_SORTED))) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(SQC_ERR_ARG, std::string("cannot open ") + path + " for writing");
+    const char magic[8] = {'S', 'Q', 'C', 'S', 'N', 'A', 'P', '1'};
+    const uint32_t hdr[2] = {nq_, dbl_ ? (uint32_t)SQC_FP64 : (uint32_t)SQC_FP32};
+    bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(hdr, 4, 2, f) == 2 && std::fwrite(&n, 8, 1, f) == 1 &&
+              std::fwrite(k.data(), 8, n, f) == n && std::fwrite(r.data(), 8, n, f) == n &&
+              std::fwrite(i.data(), 8, n, f) == n;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? SQC_OK : fail(SQC_ERR_ARG, std::string("write failed: ") + path);
+}
+
+int Engine::load(const char* path) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(SQC_ERR_ARG, std::string("cannot open ") + path);
+    char magic[8];
+    uint32_t hdr[2];
+    uint64_t n = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "SQCSNAP1", 8) == 0 &&
+              std::fread(hdr, 4, 2, f) == 2 && std::fread(&n, 8, 1, f) == 1;
+    if (ok && hdr[0] != nq_) {
+        std::fclose(f);
+        return fail(SQC_ERR_ARG, "snapshot qubit count differs from the state's");
+    }
+    std::vector<uint64_t> k;
+    std::vector<double> r, i;
+    if (ok) {
+        k.resize(n);
+        r.resize(n);
+        i.resize(n);
+        ok = std::fread(k.data(), 8, n, f) == n && std::fread(r.data(), 8, n, f) == n && std::fread(i.data(), 8, n, f) == n;
+    }
+    std::fclose(f);
+    if (!ok) return fail(SQC_ERR_ARG, std::string("not a snapshot file or truncated: ") + path);
+    return set_state(k.data(), r.data(), i.data(), n);
 }
 
 int Engine::probability(uint64_t mask, uint64_t value, double* p) {

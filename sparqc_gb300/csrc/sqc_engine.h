@@ -51,6 +51,8 @@ public:
     int probability(uint64_t mask, uint64_t value, double* p);
     int measure(uint32_t qubit, double u, int* outcome, double* p1);
     int sample(uint64_t shots, uint64_t seed, uint64_t* keys);
+    int save(const char* path);
+    int load(const char* path);
     int norm2(double* out);
     int compare(Engine& b, double* fidelity, double* max_abs_err);
     // Compare this state (a) with a table that another object owns (b, on the same device,

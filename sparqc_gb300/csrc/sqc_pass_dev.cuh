@@ -82,16 +82,18 @@ __device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, 
     pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
     pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
     const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
-    if constexpr (swap_kind(K)) {
+    const bool swap = K == KANY ? (h.op & kOpSwap) != 0 : swap_kind(K);
+    if (swap) {
         if (sat) {
-            v.amp = swap_update<T, K>(bit, pa);
+            v.amp = K == KANY ? swap_update_rt<T>(h.kind, bit, pa) : swap_update<T, K == KANY ? KX : K>(bit, pa);
             v.pres = pp;
             v.dirty = true;
         }
     } else {
         const bool any = v.pres || pp;
         if (warp_needs<T>(sat && any)) {
-            const Cx<T> o = branch_update<T, K>(g, bit, v.amp, pa);
+            const Cx<T> o = K == KANY ? branch_update_rt<T>(h.kind, g, bit, v.amp, pa)
+                                      : branch_update<T, K == KANY ? KH : K>(g, bit, v.amp, pa);
             if (sat) {
                 const bool keep = any && !negligible(o, pb);
                 v.pres = keep;
@@ -106,9 +108,11 @@ __device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, 
 template <class T, uint32_t K>
 __device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, Val<T>& v) {
     const bool bit = slot_bit(h, v.key);
-    const bool need = v.pres && (!one_sided_kind(K) || bit) && slot_sat(h, v.key);
+    const bool one_sided = K == KANY ? (h.op & kOpOneSided) != 0 : one_sided_kind(K);
+    const bool need = v.pres && (!one_sided || bit) && slot_sat(h, v.key);
     if (warp_needs<T>(need)) {
-        const Cx<T> o = diag_update<T, K>(g, bit, v.amp);
+        const Cx<T> o = K == KANY ? diag_update_rt<T>(h.kind, g, bit, v.amp)
+                                  : diag_update<T, K == KANY ? KZ : K>(g, bit, v.amp);
         if (need) { v.amp = o; v.dirty = true; }
     }
 }
@@ -120,9 +124,12 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
                                           const PruneBits& pb) {
     const bool sat = slot_sat(h, a.key);
     const bool bit_a = (h.op & kOpFlip) != 0, bit_b = !bit_a;
-    if constexpr (swap_kind(K)) {
+    const bool swap = K == KANY ? (h.op & kOpSwap) != 0 : swap_kind(K);
+    constexpr uint32_t KS_ = K == KANY ? KX : K;
+    if (swap) {
         if (sat) {
-            const Cx<T> na = swap_update<T, K>(bit_a, b.amp), nb = swap_update<T, K>(bit_b, a.amp);
+            const Cx<T> na = K == KANY ? swap_update_rt<T>(h.kind, bit_a, b.amp) : swap_update<T, KS_>(bit_a, b.amp);
+            const Cx<T> nb = K == KANY ? swap_update_rt<T>(h.kind, bit_b, a.amp) : swap_update<T, KS_>(bit_b, a.amp);
             const bool pa = b.pres, pbr = a.pres;
             a.amp = na; b.amp = nb;
             a.pres = pa; b.pres = pbr;
@@ -131,8 +138,11 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
     } else {
         const bool any = a.pres || b.pres;
         if (warp_needs<T>(sat && any)) {
-            const Cx<T> oa = branch_update<T, K>(g, bit_a, a.amp, b.amp);
-            const Cx<T> ob = branch_update<T, K>(g, bit_b, b.amp, a.amp);
+            constexpr uint32_t KB_ = K == KANY ? KH : K;
+            const Cx<T> oa = K == KANY ? branch_update_rt<T>(h.kind, g, bit_a, a.amp, b.amp)
+                                       : branch_update<T, KB_>(g, bit_a, a.amp, b.amp);
+            const Cx<T> ob = K == KANY ? branch_update_rt<T>(h.kind, g, bit_b, b.amp, a.amp)
+                                       : branch_update<T, KB_>(g, bit_b, b.amp, a.amp);
             if (sat) {
                 const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
                 a.pres = ka; a.amp = ka ? oa : czero<T>();
@@ -147,7 +157,18 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
 template <class T, uint32_t K>
 __device__ __forceinline__ void gate_on(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b,
                                         const PruneBits& pb) {
-    if constexpr (branch_kind(K) || swap_kind(K)) {
+    if constexpr (K == KANY) {   // kind known at run time: category from the encoded op bits
+        if (h.op & kOpPair) {
+            pair_step<T, KANY>(g, h, a, b, pb);
+        } else if (h.op & kOpShfl) {
+            const int off = 1 << ((h.op >> kOpOffShift) & 7u);
+            shfl_step<T, KANY>(g, h, off, a, pb);
+            shfl_step<T, KANY>(g, h, off, b, pb);
+        } else {
+            diag_step<T, KANY>(g, h, a);
+            diag_step<T, KANY>(g, h, b);
+        }
+    } else if constexpr (branch_kind(K) || swap_kind(K)) {
         if (h.op & kOpPair) {
             pair_step<T, K>(g, h, a, b, pb);
         } else {
@@ -161,14 +182,17 @@ __device__ __forceinline__ void gate_on(const GateDesc* g, const GateHead& h, Va
     }
 }
 
-// Apply gates [g0, g1) to the two held slots. Each gate is dispatched once on its (warp-
-// uniform) kind to code specialised for that kind, and applied as its pass encoded it:
+// Apply gates [g0, g1) to the two held slots. With SPEC each gate is dispatched once on its
+// (warp-uniform) kind to code specialised for that kind; without, its category is read from
+// the encoded op bits and the kind is switched on inside the arithmetic -- less code, for the
+// persistent batch kernel whose every pass type shares one instruction cache. Each gate is
+// applied as its pass encoded it:
 // branching and swap gates on the pass's first cross-group qubit pair a with b (lane-local),
 // those on qubits 0..3 or on the second cross-group qubit pair each lane with lane ^ off (the
 // other half of the warp holds the groups with the second qubit's bit set), diagonal gates are
 // lane-local. Lane 0 accumulates the amp-update count: every gate is credited with the present
 // slots it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
-template <class T>
+template <class T, bool SPEC = true>
 __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, Val<T>& a,
                                           Val<T>& b, int lane, const PruneBits& pb, unsigned long long& upd) {
     // present slots in the warp: only a branching gate changes the count (swap gates permute
@@ -181,6 +205,10 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
         if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
         recount = (h.op & kOpBranch) != 0;
         if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        if constexpr (!SPEC) {
+            gate_on<T, KANY>(g, h, a, b, pb);
+            continue;
+        }
         switch (h.kind) {
         case KX: gate_on<T, KX>(g, h, a, b, pb); break;
         case KY: gate_on<T, KY>(g, h, a, b, pb); break;
@@ -332,7 +360,7 @@ __device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsig
 // Process the owned units of a units4 round: pairs two per warp step (one per half), quads one
 // per warp step (the half selects the q2 bit); each unit's groups are loaded straight from the
 // table, the gates applied, and the slots written back.
-template <class T, int NX>
+template <class T, int NX, bool SPEC = true>
 __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates, uint32_t g0,
                                            uint32_t g1, unsigned long long m1, unsigned long long m2, unsigned om,
                                            long long mb, unsigned long long G0,
@@ -364,7 +392,7 @@ __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* 
         const bool act = u >= 0;
         load_val_g<T>(t, va, Ga, act ? xa : -1, j);
         load_val_g<T>(t, vb, Ga | m1, act ? xb : -1, j);
-        run_gates<T>(gates, g0, g1, va, vb, lane, pb, upd);
+        run_gates<T, SPEC>(gates, g0, g1, va, vb, lane, pb, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         append_new(t, ctl, fa, fb, lane);

@@ -22,7 +22,8 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_apply_gates", "sqc_x", "sqc_y", "sqc_z", "sqc_h", "sqc_phase", "sqc_rz", "sqc_rx", "sqc_ry",
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
-           "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample",
+           "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
+           "sqc_load",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_autotune", "sqc_batch_get_stats", "sqc_batch_compare", "sqc_batch_last_error",
@@ -133,7 +134,11 @@ def load(path=LIB_PATH):
     L.sqc_probability.argtypes = [P, U64, U64, ctypes.POINTER(D)]
     L.sqc_measure.argtypes = [P, U32, D, ctypes.POINTER(I), ctypes.POINTER(D)]
     L.sqc_sample.argtypes = [P, U64, U64, P]
-    for n in ("sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample"):
+    L.sqc_swap.argtypes = [P, U32, U32]
+    L.sqc_save.argtypes = [P, ctypes.c_char_p]
+    L.sqc_load.argtypes = [P, ctypes.c_char_p]
+    for n in ("sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
+              "sqc_load"):
         getattr(L, n).restype = I
     L.sqc_status_string.argtypes = [I]
     L.sqc_status_string.restype = ctypes.c_char_p
@@ -316,6 +321,15 @@ class State:
         out = np.empty(max(shots, 1), np.uint64)
         self._check(self._L.sqc_sample(self._h, shots, seed, _p(out)), "sample")
         return out[:shots]
+
+    def swap(self, a, b):
+        self._check(self._L.sqc_swap(self._h, a, b), "swap")
+
+    def save(self, path):
+        self._check(self._L.sqc_save(self._h, os.fsencode(path)), "save")
+
+    def load(self, path):
+        self._check(self._L.sqc_load(self._h, os.fsencode(path)), "load")
 
     def norm2(self):
         v = ctypes.c_double()
