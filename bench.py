@@ -45,7 +45,7 @@ def parse_args():
     ap.add_argument("--circuits", type=int, default=256, help="c4: circuits per batch")
     ap.add_argument("--autotune", action="store_true", help="c4: autotune the batch before timing")
     ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
-    ap.add_argument("--rates", type=str, default="10,40", help="c5: arrival rates (circuits/s), comma-separated")
+    ap.add_argument("--rates", type=str, default="50,1000", help="c5: arrival rates (circuits/s), comma-separated")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: table memory budget")
     ap.add_argument("--slice-ms", type=float, default=2.0, help="c5: serving time slice")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])

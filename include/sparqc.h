@@ -309,13 +309,18 @@ typedef struct sqc_server_options {
     uint32_t max_slots;        /* circuits resident at once, default 1024 */
     uint32_t min_chunk;        /* default 8 */
     double slice_ms;           /* device time of one step before running circuits park, default 2 */
-    uint32_t reserved[6];
+    uint32_t solo_log2_groups; /* circuits that can hold 2^x or more 16-key groups run alone on the
+                                  single-state engine (pipelined large-table passes), a slice of
+                                  their gates per step; 0 = default (17), 64 = never */
+    uint32_t solo_share_pct;   /* percent of the budget kept for those circuits' tables, default 25 */
+    uint32_t reserved[4];
 } sqc_server_options;
 
 enum { SQC_REQ_QUEUED = 0, SQC_REQ_RUNNING = 1, SQC_REQ_DONE = 2 };
 
 typedef struct sqc_server_stats {
     uint64_t queued, running, completed;   /* requests in each state (completed: not yet released) */
+    uint64_t solo_running;                 /* running requests on the single-state engine */
     uint64_t steps;                        /* steps that launched work */
     uint64_t kernel_launches;
     uint64_t amp_updates;                  /* of the requests completed so far */

@@ -140,7 +140,9 @@ void sqc_server_default_options(sqc_server_options* opt) {
     opt->max_slots = 1024;
     opt->min_chunk = 8;
     opt->slice_ms = 2.0;
-    for (int i = 0; i < 6; ++i) opt->reserved[i] = 0;
+    opt->solo_log2_groups = 0;
+    opt->solo_share_pct = 25;
+    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_server_create(const sqc_server_options* opt, sqc_server** out) {
@@ -208,6 +210,11 @@ int sqc_server_get_stats(sqc_server* sv, sqc_server_stats* out) {
 int sqc_server_compare(sqc_server* sv, uint64_t id, sqc_state* ref, double* fidelity, double* max_abs_err) {
     if (!ref || !fidelity || !max_abs_err) return SQC_ERR_ARG;
     return guarded(sv, [&](sqc::Server& s) {
+        if (sqc::Engine* e = s.solo_engine(id)) {
+            const int rc = ref->eng.compare(*e, fidelity, max_abs_err);
+            if (rc) s.err = ref->eng.err;
+            return rc;
+        }
         sqc::TableDev t;
         const sqc::Ctl* c = nullptr;
         unsigned long long hint = 0, frame = 0;

@@ -25,8 +25,10 @@ Server::~Server() {
         if (p) cudaFree(p);
     for (void* p : {(void*)h_circ_, (void*)h_ctl_, (void*)h_sched_, (void*)h_cmd_, (void*)h_limit_, (void*)h_bctl_})
         if (p) cudaFreeHost(p);
+    reqs_.clear();   // solo engines release their tables before the stream goes
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    if (ev2_) cudaEventDestroy(ev2_);
     if (own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -51,8 +53,13 @@ int Server::init(const sqc_server_options* opt) {
     if (o.min_chunk == 0 || (o.min_chunk & 3) || o.min_chunk > 4096) return fail(SQC_ERR_ARG, "bad min_chunk");
     if (o.max_slots == 0 || o.max_slots > (1u << 16)) return fail(SQC_ERR_ARG, "max_slots must be 1..65536");
     if (!(o.slice_ms > 0.0)) return fail(SQC_ERR_ARG, "slice_ms must be positive");
+    if (o.solo_log2_groups > 64) return fail(SQC_ERR_ARG, "solo_log2_groups must be 0..64");
+    if (o.solo_share_pct > 90) return fail(SQC_ERR_ARG, "solo_share_pct must be 0..90");
     dbl_ = o.precision == SQC_FP64;
     lf_ = o.load_factor;
+    prune_thr_ = o.prune_threshold;
+    const uint32_t sl = o.solo_log2_groups ? o.solo_log2_groups : 17;
+    solo_min_groups_ = sl >= 64 ? ~0ULL : (1ULL << sl);
     min_chunk_ = o.min_chunk;
     max_slots_ = o.max_slots;
     slice_ms_ = o.slice_ms;
@@ -68,9 +75,12 @@ int Server::init(const sqc_server_options* opt) {
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_);
     size_t free_b = 0, total_b = 0;
     if ((rc = cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
-    size_t budget = o.memory_budget ? (size_t)o.memory_budget
-                                    : (size_t)std::min(kDefaultBudget, 0.9 * (double)total_b);
-    if (budget > free_b) return fail(SQC_ERR_BUDGET, "memory budget exceeds the free device memory");
+    const size_t total_budget = o.memory_budget ? (size_t)o.memory_budget
+                                                : (size_t)std::min(kDefaultBudget, 0.9 * (double)total_b);
+    if (total_budget > free_b) return fail(SQC_ERR_BUDGET, "memory budget exceeds the free device memory");
+    // the slice pool takes the budget but the share kept for solo circuits' own tables
+    solo_cap_ = solo_min_groups_ == ~0ULL ? 0 : (size_t)((double)total_budget * o.solo_share_pct / 100.0);
+    const size_t budget = total_budget - solo_cap_;
     if (o.stream) {
         stream_ = (cudaStream_t)o.stream;
     } else {
@@ -96,7 +106,8 @@ int Server::init(const sqc_server_options* opt) {
         (rc = cuda(cudaMemset(d_sched_, 0, n * sizeof(BSched)), "cudaMemset")) ||
         (rc = cuda(cudaMemset(d_words_, 0, n * sizeof(unsigned long long)), "cudaMemset")) ||
         (rc = cuda(cudaMemset(d_bctl_, 0, sizeof(BatchCtl)), "cudaMemset")) ||
-        (rc = cuda(cudaEventCreate(&ev0_), "event")) || (rc = cuda(cudaEventCreate(&ev1_), "event")))
+        (rc = cuda(cudaEventCreate(&ev0_), "event")) || (rc = cuda(cudaEventCreate(&ev1_), "event")) ||
+        (rc = cuda(cudaEventCreate(&ev2_), "event")))
         return rc;
     std::memset(h_circ_, 0, n * sizeof(BCirc));
     std::memset(h_cmd_, 0, n * sizeof(unsigned));
@@ -118,8 +129,12 @@ int Server::submit(const sqc_circuit_desc* c, uint64_t* id) {
     Request r;
     if (const char* why = plan_circuit(c->nq, c->gates, c->n_gates, kMaxRun, 2, &r.plan)) return fail(SQC_ERR_ARG, why);
     r.nb = slice_buckets(r.plan.bound, lf_);
-    if (!r.nb || request_bytes(r) > alloc_.size())
+    r.solo = r.plan.bound >= solo_min_groups_ && r.nb && solo_bytes(r) <= solo_cap_;
+    if (r.solo) {
+        r.gates.assign(c->gates, c->gates + c->n_gates);
+    } else if (!r.nb || request_bytes(r) > alloc_.size()) {
         return fail(SQC_ERR_BUDGET, "the circuit's table slice can never fit the memory budget");
+    }
     const uint64_t rid = next_id_++;
     reqs_.emplace(rid, std::move(r));
     queue_.push_back(rid);
@@ -127,12 +142,51 @@ int Server::submit(const sqc_circuit_desc* c, uint64_t* id) {
     return SQC_OK;
 }
 
-// Admit queued requests in arrival order while a slot and pool memory are free.
+// Device bytes of a solo circuit's engine tables (sized so they never grow).
+size_t Server::solo_bytes(const Request& r) const {
+    const size_t per = sizeof(Header) + kSlots * 8 + kSlots * (dbl_ ? 16 : 8) + 4 + sizeof(Unit);
+    return (size_t)r.nb * per;
+}
+
+int Server::admit_solo(uint64_t rid, Request& r) {
+    sqc_options o;
+    sqc_default_options(&o);
+    o.precision = dbl_ ? SQC_FP64 : SQC_FP32;
+    o.prune_threshold = prune_thr_;
+    o.initial_buckets = r.nb;
+    o.stream = stream_;
+    o.device = (uint32_t)device_;
+    sqc_hash_table_parameters hp;
+    std::memset(&hp, 0, sizeof hp);
+    hp.N_devices = 1;
+    hp.coef_gpu_memory_reserve = 0.0;
+    r.eng.reset(new Engine());
+    int rc = r.eng->init(r.plan.nq, &hp, &o);
+    if (rc) {
+        err = "solo engine: " + r.eng->err;
+        r.eng.reset();
+        return rc;
+    }
+    solo_used_ += solo_bytes(r);
+    r.state = SQC_REQ_RUNNING;
+    solo_.push_back(rid);
+    return SQC_OK;
+}
+
+// Admit queued requests in arrival order while a slot and pool memory are free (solo circuits:
+// while the solo share of the budget has room).
 int Server::admit() {
     int rc;
-    while (!queue_.empty() && !free_slots_.empty()) {
+    while (!queue_.empty()) {
         const uint64_t rid = queue_.front();
         Request& r = reqs_.at(rid);
+        if (r.solo) {
+            if (solo_used_ + solo_bytes(r) > solo_cap_) break;
+            if ((rc = admit_solo(rid, r))) return rc;
+            queue_.pop_front();
+            continue;
+        }
+        if (free_slots_.empty()) break;
         const size_t bytes = request_bytes(r);
         const size_t off = alloc_.alloc(bytes);
         if (off == SIZE_MAX) break;
@@ -200,29 +254,76 @@ int Server::step(uint32_t* finished) {
     bool any = false;
     for (uint32_t s = 0; s < n_used_ && !any; ++s)
         any = slot_req_[s] && reqs_.at(slot_req_[s]).state == SQC_REQ_RUNNING;
-    if (!any) return cuda(cudaStreamSynchronize(stream_), "sync");
+    if (!any && solo_.empty()) return cuda(cudaStreamSynchronize(stream_), "sync");
     const uint32_t n = n_used_;
-    if ((rc = cuda(cudaMemcpyAsync(d_circ_, h_circ_, n * sizeof(BCirc), cudaMemcpyHostToDevice, stream_), "H2D")) ||
-        (rc = cuda(cudaMemcpyAsync(d_cmd_, h_cmd_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "H2D")) ||
-        (rc = cuda(cudaMemcpyAsync(d_limit_, h_limit_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "H2D")))
+    if ((rc = cuda(cudaEventRecord(ev0_, stream_), "event"))) return rc;
+    if (any) {
+        // the small circuits: one time slice of the persistent kernel over the resident slots
+        if ((rc = cuda(cudaMemcpyAsync(d_circ_, h_circ_, n * sizeof(BCirc), cudaMemcpyHostToDevice, stream_), "H2D")) ||
+            (rc = cuda(cudaMemcpyAsync(d_cmd_, h_cmd_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "H2D")) ||
+            (rc = cuda(cudaMemcpyAsync(d_limit_, h_limit_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_),
+                       "H2D")))
+            return rc;
+        const int grid = sms_ * batch_residency(dbl_, 0);
+        const unsigned long long slice_ns = (unsigned long long)(slice_ms_ * 1e6);
+        if ((rc = cuda(launch_batch(args(n), dbl_, grid, 0, slice_ns, stream_), "batch launch")) ||
+            (rc = cuda(cudaMemcpyAsync(h_sched_, d_sched_, n * sizeof(BSched), cudaMemcpyDeviceToHost, stream_), "D2H")) ||
+            (rc = cuda(cudaMemcpyAsync(h_ctl_, d_ctl_, n * sizeof(Ctl), cudaMemcpyDeviceToHost, stream_), "D2H")) ||
+            (rc = cuda(cudaMemcpyAsync(h_bctl_, d_bctl_, sizeof(BatchCtl), cudaMemcpyDeviceToHost, stream_), "D2H")))
+            return rc;
+        launches_ += 2;
+    }
+    if ((rc = cuda(cudaEventRecord(ev1_, stream_), "event"))) return rc;
+    // the large circuits: each applies as many of its next gates as fit a time slice at the
+    // rate measured on its previous steps
+    for (uint64_t rid : solo_) {
+        Request& r = reqs_.at(rid);
+        const uint64_t left = r.gates.size() - r.pos;
+        uint64_t g = r.ms_per_gate > 0.0 ? (uint64_t)(slice_ms_ / r.ms_per_gate) : 32;
+        g = std::min<uint64_t>(std::max<uint64_t>(8, g), left);
+        r.chunk = g;
+        if (g && (rc = r.eng->apply(r.gates.data() + r.pos, g))) { err = r.eng->err; return rc; }
+        if ((rc = r.eng->flush())) { err = r.eng->err; return rc; }
+    }
+    if ((rc = cuda(cudaEventRecord(ev2_, stream_), "event")) || (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
         return rc;
-    const int grid = sms_ * batch_residency(dbl_, 0);
-    const unsigned long long slice_ns = (unsigned long long)(slice_ms_ * 1e6);
-    if ((rc = cuda(cudaEventRecord(ev0_, stream_), "event")) ||
-        (rc = cuda(launch_batch(args(n), dbl_, grid, 0, slice_ns, stream_), "batch launch")) ||
-        (rc = cuda(cudaEventRecord(ev1_, stream_), "event")) ||
-        (rc = cuda(cudaMemcpyAsync(h_sched_, d_sched_, n * sizeof(BSched), cudaMemcpyDeviceToHost, stream_), "D2H")) ||
-        (rc = cuda(cudaMemcpyAsync(h_ctl_, d_ctl_, n * sizeof(Ctl), cudaMemcpyDeviceToHost, stream_), "D2H")) ||
-        (rc = cuda(cudaMemcpyAsync(h_bctl_, d_bctl_, sizeof(BatchCtl), cudaMemcpyDeviceToHost, stream_), "D2H")) ||
-        (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
-        return rc;
-    launches_ += 2;
     ++steps_;
-    float ms = 0.f;
+    float ms = 0.f, ms_solo = 0.f;
     if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) busy_ms_ += ms;
-    const bool timeout = h_bctl_->status == ST_TIMEOUT;
+    if (cudaEventElapsedTime(&ms_solo, ev1_, ev2_) == cudaSuccess) busy_ms_ += ms_solo;
     uint32_t fin = 0;
-    for (uint32_t s = 0; s < n; ++s) {
+    // solo circuits: measured rate, completion
+    uint64_t solo_gates = 0;
+    for (uint64_t rid : solo_) solo_gates += reqs_.at(rid).chunk;
+    std::vector<uint64_t> still;
+    for (uint64_t rid : solo_) {
+        Request& r = reqs_.at(rid);
+        if (solo_gates && ms_solo > 0.f) r.ms_per_gate = (double)ms_solo / (double)solo_gates;
+        r.pos += r.chunk;
+        r.chunk = 0;
+        if (r.pos < r.gates.size()) {
+            still.push_back(rid);
+            continue;
+        }
+        rc = r.eng->sync();
+        r.state = SQC_REQ_DONE;
+        r.status = rc;
+        if (rc == SQC_OK) {
+            sqc_stats es;
+            r.eng->stats(&es);
+            r.amp_updates = es.amp_updates;
+            upd_done_ += es.amp_updates;
+            uint64_t nz = 0;
+            r.eng->nnz(&nz);
+            r.ctl.nnz = nz;
+        }
+        done_.push_back(rid);
+        ++fin;
+    }
+    solo_.swap(still);
+    // batch slots
+    const bool timeout = any && h_bctl_->status == ST_TIMEOUT;
+    for (uint32_t s = 0; any && s < n; ++s) {
         const uint64_t rid = slot_req_[s];
         if (!rid) continue;
         Request& r = reqs_.at(rid);
@@ -276,6 +377,11 @@ int Server::nnz(uint64_t id, uint64_t* out) {
     return SQC_OK;
 }
 
+Engine* Server::solo_engine(uint64_t id) {
+    auto it = reqs_.find(id);
+    return it != reqs_.end() && it->second.solo && it->second.state == SQC_REQ_DONE ? it->second.eng.get() : nullptr;
+}
+
 int Server::get_state(uint64_t id, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
     auto it = reqs_.find(id);
     if (it == reqs_.end()) return fail(SQC_ERR_ARG, "unknown request");
@@ -283,6 +389,11 @@ int Server::get_state(uint64_t id, uint64_t* keys, double* re, double* im, uint6
     if (r.state != SQC_REQ_DONE) return fail(SQC_ERR_STATE, "request not completed");
     if (r.status != SQC_OK) return fail(r.status, "the request failed");
     int rc;
+    if (r.solo) {
+        rc = r.eng->get_state(keys, re, im, cap, n, flags);
+        if (rc) err = r.eng->err;
+        return rc;
+    }
     const unsigned long long have = r.ctl.nnz;
     if (have > rcap_) {
         const size_t c = std::max<size_t>(have, 1024);
@@ -337,6 +448,7 @@ int Server::table_of(uint64_t id, TableDev* t, const Ctl** ctl, unsigned long lo
     const Request& r = it->second;
     if (r.state != SQC_REQ_DONE) return fail(SQC_ERR_STATE, "request not completed");
     if (r.status != SQC_OK) return fail(r.status, "the request failed");
+    if (r.solo) return fail(SQC_ERR_STATE, "request ran on its own engine");
     *t = r.table;
     *ctl = d_ctl_ + r.slot;
     *hint = r.ctl.list_n;
@@ -351,6 +463,12 @@ int Server::release(uint64_t id) {
     if (it == reqs_.end()) return fail(SQC_ERR_ARG, "unknown request");
     Request& r = it->second;
     if (r.state != SQC_REQ_DONE) return fail(SQC_ERR_STATE, "only completed requests can be released");
+    if (r.solo) {
+        solo_used_ -= solo_bytes(r);
+        done_.erase(std::remove(done_.begin(), done_.end(), id), done_.end());
+        reqs_.erase(it);   // the engine frees its tables
+        return SQC_OK;
+    }
     const int slot = r.slot;
     alloc_.release(r.off, r.bytes);
     std::memset(&h_circ_[slot], 0, sizeof(BCirc));
@@ -368,12 +486,13 @@ int Server::stats(sqc_server_stats* out) {
     std::memset(out, 0, sizeof *out);
     out->queued = queue_.size();
     for (auto& kv : reqs_) out->running += kv.second.state == SQC_REQ_RUNNING ? 1 : 0;
+    out->solo_running = solo_.size();
     out->completed = done_.size();
     out->steps = steps_;
     out->kernel_launches = launches_;
     out->amp_updates = upd_done_;
-    out->pool_bytes = alloc_.size();
-    out->pool_used = alloc_.used();
+    out->pool_bytes = alloc_.size() + solo_cap_;
+    out->pool_used = alloc_.used() + solo_used_;
     out->busy_ms = busy_ms_;
     return SQC_OK;
 }

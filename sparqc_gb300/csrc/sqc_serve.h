@@ -9,6 +9,7 @@
 #pragma once
 #include <cstdint>
 #include <deque>
+#include <memory>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -16,6 +17,7 @@
 
 #include "../../include/sparqc.h"
 #include "sqc_batch.h"
+#include "sqc_engine.h"
 #include "sqc_pool.h"
 
 namespace sqc {
@@ -42,6 +44,8 @@ public:
     // completed request (for comparisons against another state).
     int table_of(uint64_t id, TableDev* t, const Ctl** ctl, unsigned long long* hint, unsigned long long* frame,
                  uint32_t* nq, bool* dbl);
+    // The engine of a completed request that ran alone (large circuits), else nullptr.
+    Engine* solo_engine(uint64_t id);
 
     std::string err;
 
@@ -55,12 +59,22 @@ private:
         unsigned long long nb = 0;
         TableDev table{};
         Ctl ctl{};                   // control block copied back when the request completed
+        // a large circuit runs alone on a single-state engine, a slice of its gates per step
+        bool solo = false;
+        std::unique_ptr<Engine> eng;
+        std::vector<sqc_gate> gates;
+        uint64_t pos = 0;            // gates applied so far
+        uint64_t chunk = 0;          // gates applied in the running step
+        double ms_per_gate = 0.0;    // measured on the previous steps
+        uint64_t amp_updates = 0;
     };
 
     int fail(int code, const std::string& msg);
     int cuda(cudaError_t e, const char* what);
     size_t request_bytes(const Request& r) const;
     int admit();
+    int admit_solo(uint64_t rid, Request& r);
+    size_t solo_bytes(const Request& r) const;
     BatchArgs args(uint32_t n) const;
 
     int device_ = 0;
@@ -71,6 +85,10 @@ private:
     uint32_t min_chunk_ = 8;
     uint32_t max_slots_ = 1024;
     double slice_ms_ = 2.0;
+    unsigned long long solo_min_groups_ = 1ULL << 17;
+    size_t solo_cap_ = 0, solo_used_ = 0;
+    std::vector<uint64_t> solo_;         // running solo requests, in admission order
+    double prune_thr_ = 1e-14;
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;
 
@@ -103,7 +121,7 @@ private:
     double* d_ri_ = nullptr;
     size_t rcap_ = 0;
 
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, ev2_ = nullptr;
     uint64_t steps_ = 0, launches_ = 0, upd_done_ = 0;
     double busy_ms_ = 0.0;
 };

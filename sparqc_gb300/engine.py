@@ -82,11 +82,13 @@ class ServerOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_uint32), ("device", ctypes.c_uint32), ("stream", ctypes.c_void_p),
                 ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
                 ("memory_budget", ctypes.c_uint64), ("max_slots", ctypes.c_uint32), ("min_chunk", ctypes.c_uint32),
-                ("slice_ms", ctypes.c_double), ("reserved", ctypes.c_uint32 * 6)]
+                ("slice_ms", ctypes.c_double), ("solo_log2_groups", ctypes.c_uint32),
+                ("solo_share_pct", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("queued", ctypes.c_uint64), ("running", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("solo_running", ctypes.c_uint64),
                 ("steps", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("amp_updates", ctypes.c_uint64),
                 ("pool_bytes", ctypes.c_uint64), ("pool_used", ctypes.c_uint64), ("busy_ms", ctypes.c_double)]
 
@@ -506,7 +508,7 @@ class Server:
     """
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, memory_budget=0, max_slots=1024,
-                 min_chunk=8, slice_ms=2.0, stream=None, device=0):
+                 min_chunk=8, slice_ms=2.0, stream=None, device=0, solo_log2_groups=0, solo_share_pct=25):
         self._L = load()
         o = ServerOptions()
         self._L.sqc_server_default_options(ctypes.byref(o))
@@ -517,6 +519,8 @@ class Server:
         o.max_slots = max_slots
         o.min_chunk = min_chunk
         o.slice_ms = slice_ms
+        o.solo_log2_groups = solo_log2_groups
+        o.solo_share_pct = solo_share_pct
         o.stream = stream
         o.device = device
         h = ctypes.c_void_p()

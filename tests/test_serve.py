@@ -121,3 +121,19 @@ def test_server_rejects_what_can_never_fit():
     assert sv.status(rid)[0] == REQ_DONE
     k, r, _ = sv.state(rid)
     assert k.tolist() == [0, 1] and np.allclose(r, [2 ** -0.5] * 2)
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_large_requests_run_alone_with_the_same_result(precision):
+    # circuits that can hold 2^6 groups or more run on their own engine, a slice of gates per
+    # step, beside the small ones in the persistent kernel
+    cs = _stream(16, 3)
+    big = [(30, circuits.random_circuit(30, 16, 300, 2, circuits.SplitMix64(900 + i))) for i in range(3)]
+    mix = cs[:6] + big[:1] + cs[6:12] + big[1:] + cs[12:]
+    sv = Server(precision=precision, memory_budget=512 * MB, slice_ms=0.2, solo_log2_groups=6, solo_share_pct=50)
+    got, steps = _serve(sv, mix, per_step=2)
+    assert steps > 5
+    for i, (nq, g) in enumerate(mix):
+        assert _same(got[i], _alone(nq, g, precision)), f"request {i}"
+    s = sv.stats()
+    assert s["pool_used"] == 0 and s["solo_running"] == 0
