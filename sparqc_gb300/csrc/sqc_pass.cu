@@ -85,8 +85,12 @@ __device__ __forceinline__ bool could_overflow(const PassArgs& a, unsigned long 
     return grown > a.max_groups;
 }
 
+// Blocks per SM the direct kernel's registers are sized for: FP32 fits four without spills,
+// FP64 three.
+template <class T> struct DirectOcc { static constexpr int kMin = sizeof(T) == 8 ? 3 : 4; };
+
 template <class T, int NX>
-__global__ void __launch_bounds__(kThreads, 3) direct_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kThreads, DirectOcc<T>::kMin) direct_kernel(PassArgs a) {
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
