@@ -12,12 +12,13 @@
 // This file is compiled with global loads defaulting to L2 (-dlcm=cg): a persistent kernel
 // reads, in pass p + 1, buckets that other SMs wrote in pass p, and L1 is not coherent.
 // Gate descriptors and the circuit array never change during a launch and are read through
-// the read-only path.
+// the read-only path (plain non-coherent loads, without the pass kernels' L1 priority hint).
 //
 // A warp that finds no work sleeps briefly and retries; after kIdleLimitNs without work it
 // records ST_TIMEOUT in the batch control block and returns. Parking: when the batch has a
 // deadline, a circuit whose pass ends after the deadline parks instead of opening its next
 // pass; a later launch resumes it (used by the serving loop to admit new circuits).
+#define SQC_DESC_EVICT_LAST 0
 #include "sqc_batch.h"
 #include "sqc_pass_dev.cuh"
 

@@ -156,17 +156,54 @@ __device__ __forceinline__ float neg(float x) {
     return __int_as_float(v);
 }
 
-// Coefficients are read through a pointer to the (L1-cached, warp-broadcast) descriptor.
+// Gate descriptors are read-only for a whole launch and read by every warp for every slot it
+// holds, while the table streams through the same L1: the pass kernels mark descriptor loads
+// to stay in L1 (evict_last), so the table's traffic does not push them out to L2 between
+// uses. The persistent batch kernel, whose loads default to L2 only, keeps the plain
+// non-coherent loads (SQC_DESC_EVICT_LAST 0), which measured faster there.
+#ifndef SQC_DESC_EVICT_LAST
+#define SQC_DESC_EVICT_LAST 1
+#endif
+__device__ __forceinline__ uint4 ld_desc4(const void* p) {
+#if SQC_DESC_EVICT_LAST
+    uint4 v;
+    asm("ld.global.nc.L1::evict_last.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+#else
+    return __ldg(reinterpret_cast<const uint4*>(p));
+#endif
+}
+__device__ __forceinline__ double ld_desc(const double* p) {
+#if SQC_DESC_EVICT_LAST
+    double v;
+    asm("ld.global.nc.L1::evict_last.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+__device__ __forceinline__ float ld_desc(const float* p) {
+#if SQC_DESC_EVICT_LAST
+    float v;
+    asm("ld.global.nc.L1::evict_last.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+
+// Coefficients are read through a pointer to the (L1-resident, warp-broadcast) descriptor.
 template <class T> struct Coef;
 template <> struct Coef<double> {
-    __device__ static __forceinline__ double c(const GateDesc* g) { return __ldg(&g->c); }
-    __device__ static __forceinline__ double s(const GateDesc* g) { return __ldg(&g->s); }
-    __device__ static __forceinline__ double m(const GateDesc* g, int i) { return __ldg(&g->m[i]); }
+    __device__ static __forceinline__ double c(const GateDesc* g) { return ld_desc(&g->c); }
+    __device__ static __forceinline__ double s(const GateDesc* g) { return ld_desc(&g->s); }
+    __device__ static __forceinline__ double m(const GateDesc* g, int i) { return ld_desc(&g->m[i]); }
 };
 template <> struct Coef<float> {
-    __device__ static __forceinline__ float c(const GateDesc* g) { return __ldg(&g->cf); }
-    __device__ static __forceinline__ float s(const GateDesc* g) { return __ldg(&g->sf); }
-    __device__ static __forceinline__ float m(const GateDesc* g, int i) { return __ldg(&g->mf[i]); }
+    __device__ static __forceinline__ float c(const GateDesc* g) { return ld_desc(&g->cf); }
+    __device__ static __forceinline__ float s(const GateDesc* g) { return ld_desc(&g->sf); }
+    __device__ static __forceinline__ float m(const GateDesc* g, int i) { return ld_desc(&g->mf[i]); }
 };
 
 // Branching update seen from one member of a pair, for gate kind K: a = own amplitude,

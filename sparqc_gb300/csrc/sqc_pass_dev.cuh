@@ -42,8 +42,8 @@ struct GateHead {
 
 // The descriptor's first 32 bytes in two vector loads: {kind, target, ctrl}, {cval, op, credit}.
 __device__ __forceinline__ GateHead gate_head(const GateDesc* g) {
-    const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(g));
-    const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(g) + 1);
+    const uint4 v0 = ld_desc4(g);
+    const uint4 v1 = ld_desc4(reinterpret_cast<const uint4*>(g) + 1);
     GateHead h;
     h.kind = v0.x;
     h.target = v0.y;
