@@ -353,6 +353,46 @@ int sqc_server_compare(sqc_server* s, uint64_t id, sqc_state* ref, double* fidel
 const char* sqc_server_last_error(sqc_server* s);
 void* sqc_server_stream(sqc_server* s);
 
+/* ---- states larger than the device budget ---------------------------------------------
+ * The reference's "PC" mode (part of the circuit on one GPU, circuit size > GPU memory;
+ * emulator/device/device_data.cuh:20-23), described there but not built. A partitioned state
+ * runs in one device table while it fits; when the table cannot grow within device_bytes, the
+ * state moves to host memory and the remaining gates run in windows, each partition of the
+ * keys (split by qubits >= 4 that the window's non-diagonal gates leave alone) passing through
+ * the device table in turn. Results are bit-identical to a single table. Gates are queued;
+ * sync, nnz and get_state run them. */
+typedef struct sqc_part_state sqc_part_state;
+
+typedef struct sqc_part_stats {
+    uint32_t spilled;          /* 1 while the state lives in host memory */
+    uint32_t partition_bits;   /* partition qubits of the last window */
+    uint64_t spills;           /* moves of the state from the device table to host memory */
+    uint64_t returns;          /* moves back to the device table */
+    uint64_t windows;          /* gate windows run over host partitions */
+    uint64_t bins;             /* partitions run through the device table */
+    uint64_t splits;           /* partitions split again because they outgrew the device */
+    uint64_t bytes_h2d;        /* state bytes copied host -> device (keys and amplitudes) */
+    uint64_t bytes_d2h;        /* state bytes copied device -> host */
+    uint64_t amp_updates;      /* sum over gates of input nonzeros, all partitions (after sync) */
+    uint64_t max_bin_keys;     /* largest partition loaded into the device table */
+    uint64_t table_budget;     /* device bytes the table may use */
+} sqc_part_stats;
+
+/* device_bytes: device memory for the working table (0 = the HBM budget of params). opt as for
+ * sqc_create (precision, prune threshold, load factor, stream, device). */
+int sqc_part_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt,
+                    uint64_t device_bytes, sqc_part_state** out);
+int sqc_part_destroy(sqc_part_state* st);
+int sqc_part_set_zero_state(sqc_part_state* st);
+int sqc_part_apply_gates(sqc_part_state* st, const sqc_gate* gates, uint64_t n);
+int sqc_part_sync(sqc_part_state* st);
+int sqc_part_nnz(sqc_part_state* st, uint64_t* n);
+/* As sqc_get_state (flags SQC_READ_SORTED, SQC_READ_DROP_NEGLIGIBLE). */
+int sqc_part_get_state(sqc_part_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n_out,
+                       uint32_t flags);
+int sqc_part_get_stats(sqc_part_state* st, sqc_part_stats* out);
+const char* sqc_part_last_error(sqc_part_state* st);
+
 /* ---- introspection ------------------------------------------------------------------- */
 typedef struct sqc_stats {
     uint64_t gates_applied;    /* gates executed on the device */

@@ -219,6 +219,14 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
         all_and &= keys[i];
         all_or |= keys[i];
     }
+    // groups in the input, counted as changes of key >> 4 along the array: exact when each
+    // group's keys are contiguous (as readouts emit them), an upper bound otherwise
+    unsigned long long groups = 0, prev = ~0ULL;
+    for (uint64_t i = 0; i < n; ++i) {
+        const unsigned long long g = keys[i] >> kSlotBits;
+        groups += g != prev ? 1 : 0;
+        prev = g;
+    }
     int rc;
     if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
     pending_.clear();
@@ -227,7 +235,7 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
     seq_verified_ = 0;
     desc_used_ = 0;
     const unsigned long long need =
-        pow2_at_least(std::max<unsigned long long>(kMinBuckets, (unsigned long long)std::ceil((double)n / lf_)));
+        pow2_at_least(std::max<unsigned long long>(kMinBuckets, (unsigned long long)std::ceil((double)groups / lf_)));
     if (need > tab_.nb) {
         HostTable nt;
         if ((rc = alloc_table(need, &nt))) return rc;
@@ -283,7 +291,10 @@ int Engine::flush() {
     if (desc_used_ + n > desc_cap_) {
         std::vector<sqc_gate> keep;
         keep.swap(pending_);
-        if ((rc = sync())) return rc;   // verifies everything launched, resets desc_used_
+        if ((rc = sync())) {   // verifies everything launched, resets desc_used_
+            pending_.insert(pending_.end(), keep.begin(), keep.end());   // keep them queued
+            return rc;
+        }
         pending_.swap(keep);
         if ((rc = ensure_desc(n))) return rc;
     }
@@ -493,7 +504,11 @@ int Engine::rebuild(unsigned long long nb_new) {
 int Engine::repair(size_t k) {
     const PassRec pr = passes_[k];
     const unsigned long long groups = ctl_host_->list_n;
-    const unsigned long long nb = std::max(tab_.nb * 2, pow2_at_least((unsigned long long)std::ceil(4.0 * (double)groups / kMaxLoad)));
+    unsigned long long nb = std::max(tab_.nb * 2, pow2_at_least((unsigned long long)std::ceil(4.0 * (double)groups / kMaxLoad)));
+    // near the budget, take the largest table that still fits (the pass may refuse again)
+    unsigned long long fit = tab_.nb;
+    while ((double)(fit * 2) * bucket_bytes() <= (double)budget_) fit *= 2;
+    if (nb > fit && fit > tab_.nb) nb = fit;
     int rc;
     if ((rc = rebuild(nb))) return rc;
     std::vector<sqc_gate> again(log_.begin() + (long)pr.log_begin, log_.end());
@@ -509,6 +524,36 @@ int Engine::repair(size_t k) {
     snap_log_ = 0;
     again.insert(again.end(), pending_.begin(), pending_.end());
     pending_.swap(again);
+    return SQC_OK;
+}
+
+int Engine::take_unapplied(std::vector<sqc_gate>* rest) {
+    int rc;
+    if ((rc = read_ctl())) return rc;
+    if (ctl_host_->status != ST_GROW) return fail(SQC_ERR_STATE, "no refused pass to take back");
+    const size_t k = (size_t)(ctl_host_->seq - seq_verified_);
+    if (k >= passes_.size()) return fail(SQC_ERR_STATE, "refused pass not found");
+    const PassRec pr = passes_[k];
+    rest->assign(log_.begin() + (long)pr.log_begin, log_.end());
+    rest->insert(rest->end(), pending_.begin(), pending_.end());
+    gates_applied_ -= log_.size() - pr.log_begin;
+    passes_run_ -= passes_.size() - k;
+    // every pass from k on returned without touching the state: clear the refusal
+    ctl_host_->status = ST_OK;
+    if ((rc = cuda(cudaMemcpyAsync(&ctl_->status, &ctl_host_->status, sizeof(unsigned int), cudaMemcpyHostToDevice,
+                                   stream_), "H2D status")) ||
+        (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
+        return rc;
+    plan_ = pr.snap;
+    snap_plan_ = plan_;
+    snap_log_ = 0;
+    log_.clear();
+    passes_.clear();
+    pending_.clear();
+    desc_used_ = 0;
+    seq_verified_ = ctl_host_->seq;
+    list_hint_ = std::max<unsigned long long>(ctl_host_->list_n, 1);
+    err.clear();
     return SQC_OK;
 }
 

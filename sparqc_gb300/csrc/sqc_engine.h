@@ -60,6 +60,16 @@ public:
     int compare_with(const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
                      unsigned long long frame_b, uint32_t nq_b, int device_b, double* fidelity, double* max_abs_err);
     int stats(sqc_stats* out);
+    // Lower the cap on table memory below the HBM budget (bytes; 0 keeps the budget).
+    void limit_table_bytes(size_t bytes) {
+        if (bytes && bytes < budget_) budget_ = bytes;
+    }
+    size_t table_budget() const { return budget_; }
+    size_t bucket_bytes_now() const { return bucket_bytes(); }
+    // After sync() failed with SQC_ERR_BUDGET because the table could not grow: clear the
+    // refusal and hand back the gates that did not run. The state is then the output of the
+    // last pass that ran, readable and usable as usual.
+    int take_unapplied(std::vector<sqc_gate>* rest);
     cudaStream_t stream() const { return stream_; }
     uint32_t nq() const { return nq_; }
     int device() const { return device_; }

@@ -2,6 +2,7 @@
 #pragma once
 #include "sqc_batch.h"
 #include "sqc_engine.h"
+#include "sqc_part.h"
 #include "sqc_serve.h"
 
 struct sqc_state {
@@ -14,4 +15,8 @@ struct sqc_batch {
 
 struct sqc_server {
     sqc::Server s;
+};
+
+struct sqc_part_state {
+    sqc::PartState p;
 };

@@ -31,7 +31,9 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_server_default_options", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
            "sqc_server_step", "sqc_server_completed", "sqc_server_request_status", "sqc_server_nnz",
            "sqc_server_get_state", "sqc_server_release", "sqc_server_get_stats", "sqc_server_compare",
-           "sqc_server_last_error", "sqc_server_stream")
+           "sqc_server_last_error", "sqc_server_stream",
+           "sqc_part_create", "sqc_part_destroy", "sqc_part_set_zero_state", "sqc_part_apply_gates",
+           "sqc_part_sync", "sqc_part_nnz", "sqc_part_get_state", "sqc_part_get_stats", "sqc_part_last_error")
 
 
 class HashTableParameters(ctypes.Structure):
@@ -91,6 +93,12 @@ class ServerStats(ctypes.Structure):
                 ("solo_running", ctypes.c_uint64),
                 ("steps", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("amp_updates", ctypes.c_uint64),
                 ("pool_bytes", ctypes.c_uint64), ("pool_used", ctypes.c_uint64), ("busy_ms", ctypes.c_double)]
+
+
+class PartStats(ctypes.Structure):
+    _fields_ = [("spilled", ctypes.c_uint32), ("partition_bits", ctypes.c_uint32)] + [
+        (n, ctypes.c_uint64) for n in ("spills", "returns", "windows", "bins", "splits", "bytes_h2d", "bytes_d2h",
+                                       "amp_updates", "max_bin_keys", "table_budget")]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE = 0, 1, 2
@@ -182,6 +190,20 @@ def load(path=LIB_PATH):
     L.sqc_server_last_error.restype = ctypes.c_char_p
     L.sqc_server_stream.argtypes = [P]
     L.sqc_server_stream.restype = P
+    L.sqc_part_create.argtypes = [U32, ctypes.POINTER(HashTableParameters), ctypes.POINTER(Options), U64,
+                                  ctypes.POINTER(P)]
+    L.sqc_part_destroy.argtypes = [P]
+    L.sqc_part_set_zero_state.argtypes = [P]
+    L.sqc_part_apply_gates.argtypes = [P, P, U64]
+    L.sqc_part_sync.argtypes = [P]
+    L.sqc_part_nnz.argtypes = [P, ctypes.POINTER(U64)]
+    L.sqc_part_get_state.argtypes = [P, P, P, P, U64, ctypes.POINTER(U64), U32]
+    L.sqc_part_get_stats.argtypes = [P, ctypes.POINTER(PartStats)]
+    L.sqc_part_last_error.argtypes = [P]
+    L.sqc_part_last_error.restype = ctypes.c_char_p
+    for n in ("sqc_part_create", "sqc_part_destroy", "sqc_part_set_zero_state", "sqc_part_apply_gates",
+              "sqc_part_sync", "sqc_part_nnz", "sqc_part_get_state", "sqc_part_get_stats"):
+        getattr(L, n).restype = I
     for n in ("sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare", "sqc_batch_run", "sqc_batch_sync",
               "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state", "sqc_batch_autotune",
               "sqc_batch_get_stats", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
@@ -611,3 +633,80 @@ class Server:
         s = ServerStats()
         self._check(self._L.sqc_server_get_stats(self._h, ctypes.byref(s)), "server stats")
         return {n: getattr(s, n) for n, _ in ServerStats._fields_}
+
+
+class PartState:
+    """A state that may outgrow the device: it runs in one device table while the table fits in
+    ``device_bytes`` and moves to host memory, processed partition by partition, when it does not.
+    Results are bit-identical to a single table."""
+
+    def __init__(self, nq, device_bytes=0, precision=FP64, prune_threshold=1e-14, load_factor=0.5, stream=None,
+                 device=0, params=None):
+        self._L = load()
+        o = Options()
+        self._L.sqc_default_options(ctypes.byref(o))
+        o.precision = precision
+        o.prune_threshold = prune_threshold
+        o.load_factor = load_factor
+        o.stream = stream
+        o.device = device
+        h = ctypes.c_void_p()
+        pp = ctypes.byref(params) if params is not None else None
+        rc = self._L.sqc_part_create(nq, pp, ctypes.byref(o), device_bytes, ctypes.byref(h))
+        if rc != OK:
+            raise SparqcError(rc, f"sqc_part_create: {self._L.sqc_status_string(rc).decode()}")
+        self._h = h
+        self.nq = nq
+        self.precision = precision
+
+    def _check(self, rc, what):
+        if rc != OK:
+            msg = self._L.sqc_part_last_error(self._h).decode() if self._h else ""
+            raise SparqcError(rc, f"{what}: {self._L.sqc_status_string(rc).decode()} ({msg})")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sqc_part_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_zero(self):
+        self._check(self._L.sqc_part_set_zero_state(self._h), "set_zero")
+
+    def apply(self, gates):
+        gates = np.ascontiguousarray(gates, GATE_DTYPE)
+        self._check(self._L.sqc_part_apply_gates(self._h, _p(gates), gates.size), "apply")
+
+    def sync(self):
+        self._check(self._L.sqc_part_sync(self._h), "sync")
+
+    @property
+    def nnz(self):
+        n = ctypes.c_uint64()
+        self._check(self._L.sqc_part_nnz(self._h, ctypes.byref(n)), "nnz")
+        return n.value
+
+    def state(self, sorted=True, drop_negligible=False):
+        n = self.nnz
+        keys = np.empty(max(n, 1), np.uint64)
+        re = np.empty(max(n, 1), np.float64)
+        im = np.empty(max(n, 1), np.float64)
+        got = ctypes.c_uint64()
+        flags = (READ_SORTED if sorted else 0) | (READ_DROP_NEGLIGIBLE if drop_negligible else 0)
+        self._check(self._L.sqc_part_get_state(self._h, _p(keys), _p(re), _p(im), n, ctypes.byref(got), flags),
+                    "get_state")
+        m = got.value
+        return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def stats(self):
+        s = PartStats()
+        self._check(self._L.sqc_part_get_stats(self._h, ctypes.byref(s)), "part stats")
+        return {n: getattr(s, n) for n, _ in PartStats._fields_}

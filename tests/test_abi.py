@@ -51,10 +51,11 @@ def test_struct_layouts_match(tmp_path, lib_path):
 #include <stddef.h>
 #include "sparqc.h"
 int main(void) {
-    printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sqc_gate), offsetof(sqc_gate, controls),
+    printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sqc_gate), offsetof(sqc_gate, controls),
            offsetof(sqc_gate, lambda), sizeof(sqc_options), sizeof(sqc_hash_table_parameters), sizeof(sqc_stats),
            sizeof(sqc_circuit_desc), sizeof(sqc_batch_options), sizeof(sqc_batch_tuning), sizeof(sqc_batch_stats),
-           offsetof(sqc_options, time_passes), sizeof(sqc_server_options), sizeof(sqc_server_stats));
+           offsetof(sqc_options, time_passes), sizeof(sqc_server_options), sizeof(sqc_server_stats),
+           sizeof(sqc_part_stats), offsetof(sqc_part_stats, amp_updates));
     return 0;
 }
 ''')
@@ -74,6 +75,8 @@ int main(void) {
     assert vals[10] == engine.Options.time_passes.offset
     assert vals[11] == ctypes.sizeof(engine.ServerOptions)
     assert vals[12] == ctypes.sizeof(engine.ServerStats)
+    assert vals[13] == ctypes.sizeof(engine.PartStats)
+    assert vals[14] == engine.PartStats.amp_updates.offset
 
 
 def test_cpp_dropin_header_compiles(tmp_path):
