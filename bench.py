@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--gates", type=int, default=None, help="override the workload's gate count")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--device-gb", type=float, default=0.0,
+                    help="c1-c3: run through a partitioned state whose device table may use this many GB")
     return ap.parse_args()
 
 
@@ -613,10 +615,68 @@ def run_serve(args):
     print(json.dumps(out), flush=True)
 
 
+# --------------------------------------------------------------------------------------
+# c1-c3 with the device table capped below the state: the partitioned state (sqc_part_*)
+def run_part(args):
+    import torch
+    from sparqc_gb300 import build as engine_build, engine
+    engine_build.build()
+    nq, gates, p = workload(args.workload, 0, args.k, args.gates)
+    torch.cuda.set_device(0)
+    # the same circuit in one table: its work count, time and final state
+    st = engine.State(nq, precision=args.precision, initial_buckets=1 << max(6, p["k"] - 4 + 1))
+    for _ in range(2):
+        st.set_zero()
+        t0 = time.perf_counter()
+        st.apply(gates)
+        st.sync()
+        t_one = time.perf_counter() - t0
+    s_one = st.stats()
+    upd = s_one["amp_updates"]
+    want = st.state(sorted=True)
+    st.close()
+    cap = int(args.device_gb * 1e9)
+    ps = engine.PartState(nq, device_bytes=cap, precision=args.precision)
+    times, stats = [], []
+    for i in range(max(1, args.warmup) + args.steps):
+        ps.set_zero()
+        s_before = ps.stats()
+        t0 = time.perf_counter()
+        ps.apply(gates)
+        ps.sync()
+        dt = time.perf_counter() - t0
+        if i >= max(1, args.warmup):
+            times.append(dt)
+            s_after = ps.stats()
+            stats.append({k: s_after[k] - s_before[k] for k in ("spills", "windows", "bins", "splits",
+                                                                 "bytes_h2d", "bytes_d2h")})
+    got = ps.state(sorted=True)
+    identical = all(np.array_equal(a, b) for a, b in zip(got, want))
+    s = ps.stats()
+    ps.close()
+    t = float(np.mean(times))
+    st0 = stats[-1]
+    out = {"metric": "amp-updates/s", "value": upd / t, "unit": "amp-updates/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": t * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": f"f{args.precision}", "data": "synthetic",
+           "config": dict(config_dict(args.workload, p, args.precision, 1),
+                          device_table_bytes=cap, one_table_bytes=int(s_one["table_bytes"]),
+                          timing="wall clock of apply + sync per step (host partitions in the loop)"),
+           "partitioned": dict(st0, max_bin_keys=int(s["max_bin_keys"]), nnz=int(got[0].size),
+                               link_gbs=(st0["bytes_h2d"] + st0["bytes_d2h"]) / t / 1e9,
+                               identical_to_one_table=bool(identical)),
+           "one_table": {"value": upd / t_one, "ms_per_step": t_one * 1e3, "table_bytes": int(s_one["table_bytes"])}}
+    print(json.dumps(out), flush=True)
+    if not identical:
+        raise SystemExit("partitioned state differs from the single table")
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.device_gb > 0 and args.workload in ("c1", "c2", "c3"):
+        run_part(args)
     elif args.workload == "c4":
         run_batch(args)
     elif args.workload == "c5":

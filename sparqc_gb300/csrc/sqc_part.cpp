@@ -21,18 +21,6 @@ bool non_diagonal(uint32_t kind) {
 
 int popcount64(unsigned long long x) { return __builtin_popcountll(x); }
 
-// Largest partition a set of partition bits gives over a sample of keys.
-size_t worst_bin(const std::vector<uint64_t>& sample, const std::vector<int>& bits) {
-    std::vector<size_t> cnt(size_t(1) << bits.size(), 0);
-    size_t worst = 0;
-    for (uint64_t k : sample) {
-        size_t v = 0;
-        for (size_t j = 0; j < bits.size(); ++j) v |= (size_t)((k >> bits[j]) & 1ULL) << j;
-        worst = std::max(worst, ++cnt[v]);
-    }
-    return worst;
-}
-
 // Up to kSample keys spread evenly over the runs.
 std::vector<uint64_t> sample_keys(const std::vector<const Run*>& runs) {
     uint64_t n = 0;
@@ -46,6 +34,21 @@ std::vector<uint64_t> sample_keys(const std::vector<const Run*>& runs) {
         at -= r->k.size();
     }
     return s;
+}
+
+// Bin of key k under partition bits `bits` (bit j of the bin = bit bits[j] of the key).
+inline size_t bin_of(uint64_t k, const std::vector<int>& bits) {
+    size_t v = 0;
+    for (size_t j = 0; j < bits.size(); ++j) v |= (size_t)((k >> bits[j]) & 1ULL) << j;
+    return v;
+}
+
+// Largest partition a set of partition bits gives over a sample of keys.
+size_t worst_bin(const std::vector<uint64_t>& sample, const std::vector<int>& bits) {
+    std::vector<size_t> cnt(size_t(1) << bits.size(), 0);
+    size_t worst = 0;
+    for (uint64_t k : sample) worst = std::max(worst, ++cnt[bin_of(k, bits)]);
+    return worst;
 }
 
 // Choose p bits of cand greedily, each time the one that keeps the largest sampled partition
@@ -69,10 +72,31 @@ std::vector<int> choose_bits(const std::vector<uint64_t>& sample, unsigned long 
     return bits;
 }
 
-void push_entry(Run& d, const Run& s, size_t i) {
-    d.k.push_back(s.k[i]);
-    d.r.push_back(s.r[i]);
-    d.i.push_back(s.i[i]);
+// Move the entries of the runs into 2^|bits| bins by their partition bits, in order (so each
+// group stays contiguous): one pass to size the bins, one to fill them; each run is released
+// once distributed.
+std::vector<Run> distribute(std::vector<Run>& runs, const std::vector<int>& bits) {
+    std::vector<Run> bins(size_t(1) << bits.size());
+    std::vector<size_t> cnt(bins.size(), 0);
+    for (const Run& r : runs)
+        for (uint64_t k : r.k) ++cnt[bin_of(k, bits)];
+    for (size_t v = 0; v < bins.size(); ++v) {
+        bins[v].k.resize(cnt[v]);
+        bins[v].r.resize(cnt[v]);
+        bins[v].i.resize(cnt[v]);
+        cnt[v] = 0;
+    }
+    for (Run& r : runs) {
+        for (size_t i = 0; i < r.k.size(); ++i) {
+            const size_t v = bin_of(r.k[i], bits);
+            const size_t at = cnt[v]++;
+            bins[v].k[at] = r.k[i];
+            bins[v].r[at] = r.r[i];
+            bins[v].i[at] = r.i[i];
+        }
+        r = Run();
+    }
+    return bins;
 }
 
 }  // namespace
@@ -219,9 +243,12 @@ int PartState::run_bin(Run& in, std::vector<sqc_gate> gates, unsigned long long 
     if (!cand) return fail(SQC_ERR_BUDGET, "a partition outgrew the device budget and no qubit is left to split it by");
     const std::vector<uint64_t> sample = sample_keys({&in});
     const int b = choose_bits(sample, cand, 1)[0];
-    Run lo, hi;
-    for (size_t i = 0; i < in.k.size(); ++i) push_entry(((in.k[i] >> b) & 1ULL) ? hi : lo, in, i);
+    std::vector<Run> one(1);
+    one[0] = std::move(in);
     in = Run();
+    std::vector<Run> halves = distribute(one, {b});
+    Run& lo = halves[0];
+    Run& hi = halves[1];
     lo.fill_summary();
     hi.fill_summary();
     ++splits_;
@@ -280,16 +307,8 @@ int PartState::run_windows() {
         return fail(SQC_ERR_BUDGET, "the state is larger than the device budget and too few of its qubits vary to "
                                     "partition it around the next gate");
     const std::vector<int> bits = choose_bits(sample_keys(rp), varying & ~touched, p);
-    const size_t nbins = size_t(1) << bits.size();
-    std::vector<Run> bins(nbins);
-    for (Run& r : runs_) {
-        for (size_t i = 0; i < r.k.size(); ++i) {
-            size_t v = 0;
-            for (size_t j = 0; j < bits.size(); ++j) v |= (size_t)((r.k[i] >> bits[j]) & 1ULL) << j;
-            push_entry(bins[v], r, i);
-        }
-        r = Run();
-    }
+    std::vector<Run> bins = distribute(runs_, bits);
+    const size_t nbins = bins.size();
     runs_.clear();
     unsigned long long pmask = 0;
     for (int q : bits) pmask |= 1ULL << q;
