@@ -211,21 +211,29 @@ int Engine::set_zero() {
     return rc;
 }
 
-int Engine::set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n) {
+int Engine::set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n,
+                      const KeySummary* known) {
     if (n && (!keys || !re || !im)) return fail(SQC_ERR_ARG, "null array");
-    unsigned long long all_and = ~0ULL, all_or = 0;
-    for (uint64_t i = 0; i < n; ++i) {
-        if (nq_ < 64 && (keys[i] >> nq_)) return fail(SQC_ERR_ARG, "key does not fit in nq bits");
-        all_and &= keys[i];
-        all_or |= keys[i];
-    }
-    // groups in the input, counted as changes of key >> 4 along the array: exact when each
-    // group's keys are contiguous (as readouts emit them), an upper bound otherwise
-    unsigned long long groups = 0, prev = ~0ULL;
-    for (uint64_t i = 0; i < n; ++i) {
-        const unsigned long long g = keys[i] >> kSlotBits;
-        groups += g != prev ? 1 : 0;
-        prev = g;
+    unsigned long long all_and = ~0ULL, all_or = 0, groups = 0;
+    if (known) {
+        all_and = known->all_and;
+        all_or = known->all_or;
+        groups = known->groups;
+        if (nq_ < 64 && (all_or >> nq_)) return fail(SQC_ERR_ARG, "key does not fit in nq bits");
+    } else {
+        for (uint64_t i = 0; i < n; ++i) {
+            if (nq_ < 64 && (keys[i] >> nq_)) return fail(SQC_ERR_ARG, "key does not fit in nq bits");
+            all_and &= keys[i];
+            all_or |= keys[i];
+        }
+        // groups in the input, counted as changes of key >> 4 along the array: exact when each
+        // group's keys are contiguous (as readouts emit them), an upper bound otherwise
+        unsigned long long prev = ~0ULL;
+        for (uint64_t i = 0; i < n; ++i) {
+            const unsigned long long g = keys[i] >> kSlotBits;
+            groups += g != prev ? 1 : 0;
+            prev = g;
+        }
     }
     int rc;
     if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;

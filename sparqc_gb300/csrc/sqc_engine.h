@@ -39,7 +39,13 @@ public:
 
     int init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt);
     int set_zero();
-    int set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n);
+    // What a caller already knows about the keys it loads: their AND, their OR and their
+    // group count (changes of key >> 4 along the array). With it set_state skips its scans.
+    struct KeySummary {
+        unsigned long long all_and, all_or, groups;
+    };
+    int set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n,
+                  const KeySummary* known = nullptr);
     int apply(const sqc_gate* gates, uint64_t n);
     int flush();
     int sync();

@@ -3,8 +3,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
-#include <numeric>
+#include <thread>
+
+#include <cuda_runtime.h>
 
 #include "sqc_plan.h"
 
@@ -14,6 +17,7 @@ namespace {
 
 constexpr unsigned long long kLowBits = (1ULL << kSlotBits) - 1;   // qubits 0..3: inside a group
 constexpr size_t kSample = 4096;                                   // keys sampled to balance splits
+constexpr uint64_t kChunk = 1 << 20;                               // entries per host work item
 
 bool non_diagonal(uint32_t kind) {
     return kind == SQC_X || kind == SQC_Y || kind == SQC_H || kind == SQC_RX || kind == SQC_RY || kind == SQC_U;
@@ -21,19 +25,21 @@ bool non_diagonal(uint32_t kind) {
 
 int popcount64(unsigned long long x) { return __builtin_popcountll(x); }
 
-// Up to kSample keys spread evenly over the runs.
-std::vector<uint64_t> sample_keys(const std::vector<const Run*>& runs) {
-    uint64_t n = 0;
-    for (const Run* r : runs) n += r->k.size();
-    std::vector<uint64_t> s;
-    if (!n) return s;
-    const uint64_t step = std::max<uint64_t>(1, n / kSample);
-    uint64_t at = 0;
-    for (const Run* r : runs) {
-        for (; at < r->k.size(); at += step) s.push_back(r->k[at]);
-        at -= r->k.size();
+// Run f(item) for items [0, n) on up to `threads` threads (inline when there is one item).
+template <class F>
+void parallel_items(size_t n, int threads, F&& f) {
+    const size_t nt = std::min<size_t>(n, (size_t)std::max(1, threads));
+    if (nt <= 1) {
+        for (size_t i = 0; i < n; ++i) f(i);
+        return;
     }
-    return s;
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (size_t t = 0; t < nt; ++t)
+        pool.emplace_back([&, t]() {
+            for (size_t i = t; i < n; i += nt) f(i);
+        });
+    for (std::thread& th : pool) th.join();
 }
 
 // Bin of key k under partition bits `bits` (bit j of the bin = bit bits[j] of the key).
@@ -49,6 +55,21 @@ size_t worst_bin(const std::vector<uint64_t>& sample, const std::vector<int>& bi
     size_t worst = 0;
     for (uint64_t k : sample) worst = std::max(worst, ++cnt[bin_of(k, bits)]);
     return worst;
+}
+
+// Up to kSample keys spread evenly over the runs.
+std::vector<uint64_t> sample_keys(const std::vector<const Run*>& runs) {
+    uint64_t n = 0;
+    for (const Run* r : runs) n += r->n;
+    std::vector<uint64_t> s;
+    if (!n) return s;
+    const uint64_t step = std::max<uint64_t>(1, n / kSample);
+    uint64_t at = 0;
+    for (const Run* r : runs) {
+        for (; at < r->n; at += step) s.push_back(r->k[at]);
+        at -= r->n;
+    }
+    return s;
 }
 
 // Choose p bits of cand greedily, each time the one that keeps the largest sampled partition
@@ -72,48 +93,123 @@ std::vector<int> choose_bits(const std::vector<uint64_t>& sample, unsigned long 
     return bits;
 }
 
-// Move the entries of the runs into 2^|bits| bins by their partition bits, in order (so each
-// group stays contiguous): one pass to size the bins, one to fill them; each run is released
-// once distributed.
-std::vector<Run> distribute(std::vector<Run>& runs, const std::vector<int>& bits) {
-    std::vector<Run> bins(size_t(1) << bits.size());
-    std::vector<size_t> cnt(bins.size(), 0);
-    for (const Run& r : runs)
-        for (uint64_t k : r.k) ++cnt[bin_of(k, bits)];
-    for (size_t v = 0; v < bins.size(); ++v) {
-        bins[v].k.resize(cnt[v]);
-        bins[v].r.resize(cnt[v]);
-        bins[v].i.resize(cnt[v]);
-        cnt[v] = 0;
-    }
-    for (Run& r : runs) {
-        for (size_t i = 0; i < r.k.size(); ++i) {
-            const size_t v = bin_of(r.k[i], bits);
-            const size_t at = cnt[v]++;
-            bins[v].k[at] = r.k[i];
-            bins[v].r[at] = r.r[i];
-            bins[v].i[at] = r.i[i];
-        }
-        r = Run();
-    }
-    return bins;
+// A contiguous piece of a run, the unit of host work.
+struct Piece {
+    size_t run;
+    uint64_t b, e;
+};
+
+std::vector<Piece> pieces_of(const std::vector<Run>& runs) {
+    std::vector<Piece> ps;
+    for (size_t r = 0; r < runs.size(); ++r)
+        for (uint64_t b = 0; b < runs[r].n; b += kChunk) ps.push_back(Piece{r, b, std::min(runs[r].n, b + kChunk)});
+    return ps;
 }
 
 }  // namespace
 
-void Run::fill_summary() {
-    groups = 0;
-    all_and = ~0ULL;
-    all_or = 0;
-    unsigned long long prev = ~0ULL;
-    for (uint64_t key : k) {
-        const unsigned long long g = key >> kSlotBits;
-        groups += g != prev ? 1 : 0;
-        prev = g;
-        all_and &= key;
-        all_or |= key;
+// ---- pinned pool and runs ----------------------------------------------------------------
+
+PinnedPool::~PinnedPool() {
+    for (auto& kv : blocks_) {
+        if (kv.second.pinned) cudaFreeHost(kv.first);
+        else std::free(kv.first);
     }
 }
+
+void* PinnedPool::get(size_t bytes) {
+    bytes = std::max<size_t>(bytes, 64);
+    auto it = free_.lower_bound(bytes);
+    if (it != free_.end() && it->first <= 2 * bytes + (size_t(1) << 20)) {   // a cached block, not far too big
+        void* p = it->second;
+        free_.erase(it);
+        return p;
+    }
+    const size_t cap = (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+    void* p = nullptr;
+    if (cudaMallocHost(&p, cap) == cudaSuccess && p) {
+        blocks_[p] = Block{cap, true};
+        return p;
+    }
+    cudaGetLastError();   // clear the failed pin
+    while (!free_.empty()) {   // give cached blocks back before going to pageable memory
+        auto f = free_.begin();
+        if (blocks_[f->second].pinned) cudaFreeHost(f->second);
+        else std::free(f->second);
+        blocks_.erase(f->second);
+        free_.erase(f);
+    }
+    if (cudaMallocHost(&p, cap) == cudaSuccess && p) {
+        blocks_[p] = Block{cap, true};
+        return p;
+    }
+    cudaGetLastError();
+    p = std::malloc(cap);
+    if (p) blocks_[p] = Block{cap, false};
+    return p;
+}
+
+void PinnedPool::put(void* p) {
+    auto it = blocks_.find(p);
+    if (it != blocks_.end()) free_.emplace(it->second.bytes, p);
+}
+
+void Run::take(Run& o) {
+    k = o.k; r = o.r; i = o.i; n = o.n;
+    groups = o.groups; all_and = o.all_and; all_or = o.all_or;
+    pool_ = o.pool_; block_ = o.block_;
+    o.k = nullptr; o.r = nullptr; o.i = nullptr; o.n = 0;
+    o.groups = 0; o.all_and = ~0ULL; o.all_or = 0;
+    o.pool_ = nullptr; o.block_ = nullptr;
+}
+
+bool Run::alloc(PinnedPool* pool, uint64_t count) {
+    release();
+    void* b = pool->get((size_t)count * 24);
+    if (!b) return false;
+    pool_ = pool;
+    block_ = b;
+    k = static_cast<uint64_t*>(b);
+    r = reinterpret_cast<double*>(k + count);
+    i = r + count;
+    n = count;
+    return true;
+}
+
+void Run::release() {
+    if (block_ && pool_) pool_->put(block_);
+    block_ = nullptr;
+    pool_ = nullptr;
+    k = nullptr; r = nullptr; i = nullptr; n = 0;
+    groups = 0; all_and = ~0ULL; all_or = 0;
+}
+
+void Run::fill_summary(int threads) {
+    const size_t nc = (size_t)((n + kChunk - 1) / kChunk);
+    std::vector<unsigned long long> a(nc, ~0ULL), o(nc, 0), g(nc, 0);
+    parallel_items(nc, threads, [&](size_t c) {
+        const uint64_t b = c * kChunk, e = std::min<uint64_t>(n, b + kChunk);
+        unsigned long long aa = ~0ULL, oo = 0, gg = 0, prev = b ? (k[b - 1] >> kSlotBits) : ~0ULL;
+        for (uint64_t x = b; x < e; ++x) {
+            const unsigned long long key = k[x], grp = key >> kSlotBits;
+            aa &= key;
+            oo |= key;
+            gg += grp != prev ? 1 : 0;
+            prev = grp;
+        }
+        a[c] = aa; o[c] = oo; g[c] = gg;
+    });
+    all_and = ~0ULL;
+    all_or = 0;
+    groups = 0;
+    for (size_t c = 0; c < nc; ++c) {
+        all_and &= a[c];
+        all_or |= o[c];
+        groups += g[c];
+    }
+}
+
+// ---- partitioned state -------------------------------------------------------------------
 
 int PartState::fail(int code, const std::string& msg) {
     err = msg;
@@ -141,6 +237,7 @@ int PartState::init(uint32_t nq, const sqc_hash_table_parameters* params, const 
     if (rc) return from_engine(rc);
     nq_ = nq;
     thr_ = o.prune_threshold;
+    threads_ = (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
     eng_.limit_table_bytes((size_t)device_bytes);
     return SQC_OK;
 }
@@ -164,25 +261,22 @@ int PartState::read_engine(Run* out) {
     uint64_t n = 0;
     int rc = eng_.nnz(&n);
     if (rc) return from_engine(rc);
-    out->k.resize(n);
-    out->r.resize(n);
-    out->i.resize(n);
+    if (!out->alloc(&pool_, n)) return fail(SQC_ERR_OOM, "host memory for a partition");
     uint64_t got = 0;
-    if ((rc = eng_.get_state(out->k.data(), out->r.data(), out->i.data(), n, &got, 0))) return from_engine(rc);
-    out->k.resize(got);
-    out->r.resize(got);
-    out->i.resize(got);
+    if ((rc = eng_.get_state(out->k, out->r, out->i, n, &got, 0))) return from_engine(rc);
+    out->n = got;
     d2h_ += got * 24;
-    out->fill_summary();
+    out->fill_summary(threads_);
     return SQC_OK;
 }
 
 int PartState::load_engine(const Run& in) {
     take_counters();
-    const int rc = eng_.set_state(in.k.data(), in.r.data(), in.i.data(), in.k.size());
+    const Engine::KeySummary ks{in.all_and, in.all_or, in.groups};
+    const int rc = eng_.set_state(in.k, in.r, in.i, in.n, &ks);
     if (rc) return from_engine(rc);
-    h2d_ += in.k.size() * 24;
-    max_bin_ = std::max<uint64_t>(max_bin_, in.k.size());
+    h2d_ += in.n * 24;
+    max_bin_ = std::max<uint64_t>(max_bin_, in.n);
     return SQC_OK;
 }
 
@@ -191,12 +285,74 @@ int PartState::load_engine(const Run& in) {
 uint64_t PartState::bin_keys_target() const {
     uint64_t n = 0, g = 0;
     for (const Run& r : runs_) {
-        n += r.k.size();
+        n += r.n;
         g += r.groups;
     }
     const double per_group = g ? std::min(16.0, std::max(1.0, (double)n / (double)g)) : 1.0;
     const double groups_cap = (double)eng_.table_budget() / (double)eng_.bucket_bytes_now() * 0.45;
     return (uint64_t)std::max(1.0, 0.5 * groups_cap * per_group);
+}
+
+// Move the entries of the runs into 2^|bits| bins by their partition bits, keeping their order
+// (so each group stays contiguous): pieces of the runs are counted per bin in parallel, each
+// piece gets its place in every bin, and the pieces are scattered in parallel. A bin's group
+// count may count a group cut by a piece boundary twice (an upper bound, which only sizes the
+// table). The runs are released.
+int PartState::distribute(std::vector<Run>& runs, const std::vector<int>& bits, std::vector<Run>* bins) {
+    const size_t nb = size_t(1) << bits.size();
+    const std::vector<Piece> ps = pieces_of(runs);
+    std::vector<uint64_t> cnt(ps.size() * nb, 0);
+    parallel_items(ps.size(), threads_, [&](size_t c) {
+        const Piece& p = ps[c];
+        uint64_t* cc = &cnt[c * nb];
+        const uint64_t* k = runs[p.run].k;
+        for (uint64_t x = p.b; x < p.e; ++x) ++cc[bin_of(k[x], bits)];
+    });
+    bins->clear();
+    bins->resize(nb);
+    std::vector<uint64_t> off(ps.size() * nb);
+    for (size_t v = 0; v < nb; ++v) {
+        uint64_t at = 0;
+        for (size_t c = 0; c < ps.size(); ++c) {
+            off[c * nb + v] = at;
+            at += cnt[c * nb + v];
+        }
+        if (at && !(*bins)[v].alloc(&pool_, at)) return fail(SQC_ERR_OOM, "host memory for a partition");
+    }
+    std::vector<unsigned long long> a(ps.size() * nb, ~0ULL), o(ps.size() * nb, 0), g(ps.size() * nb, 0);
+    parallel_items(ps.size(), threads_, [&](size_t c) {
+        const Piece& p = ps[c];
+        const Run& src = runs[p.run];
+        std::vector<unsigned long long> prev(nb, ~0ULL);
+        for (uint64_t x = p.b; x < p.e; ++x) {
+            const unsigned long long key = src.k[x];
+            const size_t v = bin_of(key, bits);
+            Run& d = (*bins)[v];
+            const uint64_t at = off[c * nb + v]++;
+            d.k[at] = key;
+            d.r[at] = src.r[x];
+            d.i[at] = src.i[x];
+            const size_t s = c * nb + v;
+            a[s] &= key;
+            o[s] |= key;
+            const unsigned long long grp = key >> kSlotBits;
+            g[s] += grp != prev[v] ? 1 : 0;
+            prev[v] = grp;
+        }
+    });
+    for (size_t v = 0; v < nb; ++v) {
+        Run& d = (*bins)[v];
+        d.all_and = ~0ULL;
+        d.all_or = 0;
+        d.groups = 0;
+        for (size_t c = 0; c < ps.size(); ++c) {
+            d.all_and &= a[c * nb + v];
+            d.all_or |= o[c * nb + v];
+            d.groups += g[c * nb + v];
+        }
+    }
+    for (Run& r : runs) r.release();
+    return SQC_OK;
 }
 
 int PartState::apply(const sqc_gate* gates, uint64_t n) {
@@ -217,15 +373,15 @@ int PartState::apply(const sqc_gate* gates, uint64_t n) {
 // fit, at the start or at a pass that could not grow the table, is split by one more bit of
 // free_bits and each half continues with the gates that had not run.
 int PartState::run_bin(Run& in, std::vector<sqc_gate> gates, unsigned long long free_bits, std::vector<Run>* out) {
-    if (in.k.empty()) return SQC_OK;
+    if (in.n == 0) return SQC_OK;
     int rc = load_engine(in);
     if (rc && rc != SQC_ERR_BUDGET) return rc;
     if (!rc) {
+        in.release();
         if (!(rc = eng_.apply(gates.data(), gates.size()))) rc = eng_.sync();
         if (!rc) {
             Run res;
             if ((rc = read_engine(&res))) return rc;
-            in = Run();
             out->push_back(std::move(res));
             ++bins_;
             return SQC_OK;
@@ -233,27 +389,20 @@ int PartState::run_bin(Run& in, std::vector<sqc_gate> gates, unsigned long long 
         if (rc != SQC_ERR_BUDGET) return from_engine(rc);
         std::vector<sqc_gate> rest;
         if ((rc = eng_.take_unapplied(&rest))) return from_engine(rc);
-        Run cur;
-        if ((rc = read_engine(&cur))) return rc;
-        in = std::move(cur);
+        if ((rc = read_engine(&in))) return rc;
         gates.swap(rest);
         ++bins_;
     }
     const unsigned long long cand = free_bits & (in.all_or ^ in.all_and) & ~kLowBits;
     if (!cand) return fail(SQC_ERR_BUDGET, "a partition outgrew the device budget and no qubit is left to split it by");
-    const std::vector<uint64_t> sample = sample_keys({&in});
-    const int b = choose_bits(sample, cand, 1)[0];
-    std::vector<Run> one(1);
-    one[0] = std::move(in);
-    in = Run();
-    std::vector<Run> halves = distribute(one, {b});
-    Run& lo = halves[0];
-    Run& hi = halves[1];
-    lo.fill_summary();
-    hi.fill_summary();
+    const int b = choose_bits(sample_keys({&in}), cand, 1)[0];
+    std::vector<Run> one;
+    one.push_back(std::move(in));
+    std::vector<Run> halves;
+    if ((rc = distribute(one, {b}, &halves))) return rc;
     ++splits_;
-    if ((rc = run_bin(lo, gates, free_bits & ~(1ULL << b), out))) return rc;
-    return run_bin(hi, gates, free_bits & ~(1ULL << b), out);
+    if ((rc = run_bin(halves[0], gates, free_bits & ~(1ULL << b), out))) return rc;
+    return run_bin(halves[1], gates, free_bits & ~(1ULL << b), out);
 }
 
 // One window over the spilled state: partition bits, the gates they allow, every partition
@@ -263,8 +412,8 @@ int PartState::run_windows() {
     unsigned long long a = ~0ULL, o = 0;
     std::vector<const Run*> rp;
     for (const Run& r : runs_) {
-        n += r.k.size();
-        if (!r.k.empty()) {
+        n += r.n;
+        if (r.n) {
             a &= r.all_and;
             o |= r.all_or;
         }
@@ -307,18 +456,17 @@ int PartState::run_windows() {
         return fail(SQC_ERR_BUDGET, "the state is larger than the device budget and too few of its qubits vary to "
                                     "partition it around the next gate");
     const std::vector<int> bits = choose_bits(sample_keys(rp), varying & ~touched, p);
-    std::vector<Run> bins = distribute(runs_, bits);
-    const size_t nbins = bins.size();
+    std::vector<Run> bins;
+    int rc = distribute(runs_, bits, &bins);
     runs_.clear();
+    if (rc) return rc;
     unsigned long long pmask = 0;
     for (int q : bits) pmask |= 1ULL << q;
     const std::vector<sqc_gate> gates(pending_.begin(), pending_.begin() + (long)w);
     std::vector<Run> out;
-    int rc = SQC_OK;
-    for (size_t v = 0; v < nbins; ++v) {
-        bins[v].fill_summary();
+    for (size_t v = 0; v < bins.size(); ++v) {
         if (!rc) rc = run_bin(bins[v], gates, varying & ~touched & ~pmask, &out);
-        bins[v] = Run();
+        bins[v].release();
     }
     runs_.swap(out);
     if (rc) return rc;
@@ -331,26 +479,22 @@ int PartState::run_windows() {
 // Back to the device table when the whole state fits with room to grow.
 int PartState::maybe_return() {
     uint64_t n = 0;
-    for (const Run& r : runs_) n += r.k.size();
+    for (const Run& r : runs_) n += r.n;
     if (n > bin_keys_target() / 2) return SQC_OK;
     Run all;
-    all.k.reserve(n);
-    all.r.reserve(n);
-    all.i.reserve(n);
+    if (!all.alloc(&pool_, n)) return fail(SQC_ERR_OOM, "host memory for the state");
+    uint64_t at = 0;
     for (Run& r : runs_) {
-        all.k.insert(all.k.end(), r.k.begin(), r.k.end());
-        all.r.insert(all.r.end(), r.r.begin(), r.r.end());
-        all.i.insert(all.i.end(), r.i.begin(), r.i.end());
-        r = Run();
+        std::memcpy(all.k + at, r.k, r.n * 8);
+        std::memcpy(all.r + at, r.r, r.n * 8);
+        std::memcpy(all.i + at, r.i, r.n * 8);
+        at += r.n;
     }
-    runs_.clear();
+    all.fill_summary(threads_);
     const int rc = load_engine(all);
-    if (rc == SQC_ERR_BUDGET) {   // stays in host memory
-        all.fill_summary();
-        runs_.push_back(std::move(all));
-        return SQC_OK;
-    }
+    if (rc == SQC_ERR_BUDGET) return SQC_OK;   // stays in host memory
     if (rc) return rc;
+    runs_.clear();
     resident_ = true;
     ++returns_;
     return SQC_OK;
@@ -391,7 +535,7 @@ int PartState::nnz(uint64_t* out) {
     if (rc) return rc;
     if (resident_) return (rc = eng_.nnz(out)) ? from_engine(rc) : SQC_OK;
     uint64_t n = 0;
-    for (const Run& r : runs_) n += r.k.size();
+    for (const Run& r : runs_) n += r.n;
     *out = n;
     return SQC_OK;
 }
@@ -403,19 +547,17 @@ int PartState::get_state(uint64_t* keys, double* re, double* im, uint64_t cap, u
     const bool drop = (flags & SQC_READ_DROP_NEGLIGIBLE) != 0;
     // the readout filter of the device (|re| < thr and |im| < thr, decided in FP64)
     auto keep = [&](double r, double i) { return !drop || !(std::fabs(r) < thr_ && std::fabs(i) < thr_); };
-    std::vector<std::pair<uint64_t, std::pair<uint32_t, uint64_t>>> at;   // (key, (run, index))
     uint64_t got = 0;
-    for (uint32_t ri = 0; ri < runs_.size(); ++ri) {
-        const Run& r = runs_[ri];
-        for (uint64_t i = 0; i < r.k.size(); ++i) got += keep(r.r[i], r.i[i]) ? 1 : 0;
-    }
+    for (const Run& r : runs_)
+        for (uint64_t i = 0; i < r.n; ++i) got += keep(r.r[i], r.i[i]) ? 1 : 0;
     if (n) *n = got;
     if (got > cap) return fail(SQC_ERR_CAPACITY, "output arrays too small");
     if (got && (!keys || !re || !im)) return fail(SQC_ERR_ARG, "null output array");
+    std::vector<std::pair<uint64_t, std::pair<uint32_t, uint64_t>>> at;   // (key, (run, index))
     at.reserve(got);
     for (uint32_t ri = 0; ri < runs_.size(); ++ri) {
         const Run& r = runs_[ri];
-        for (uint64_t i = 0; i < r.k.size(); ++i)
+        for (uint64_t i = 0; i < r.n; ++i)
             if (keep(r.r[i], r.i[i])) at.push_back({r.k[i], {ri, i}});
     }
     if (flags & SQC_READ_SORTED)

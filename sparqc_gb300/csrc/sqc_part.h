@@ -18,10 +18,13 @@
 //    non-diagonal gates); the halves continue with the gates that had not run.
 // Qubits >= 4 keep a 16-key group inside one partition, so a partition's group count is exact
 // and its table is sized from it. When the whole state fits comfortably again, it returns to
-// the device.
+// the device. Host-side state lives in page-locked buffers (copies run at the link's speed),
+// recycled through a pool; the split of the state into partitions runs on all host cores.
 #pragma once
 #include <cstdint>
+#include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/sparqc.h"
@@ -29,13 +32,57 @@
 
 namespace sqc {
 
-// Keys (each 16-key group contiguous, as readouts emit them) and their amplitudes.
+// Page-locked host blocks, kept for reuse once released (pinning is paid once). Falls back to
+// pageable memory when the system refuses to pin more.
+class PinnedPool {
+public:
+    PinnedPool() = default;
+    PinnedPool(const PinnedPool&) = delete;
+    PinnedPool& operator=(const PinnedPool&) = delete;
+    ~PinnedPool();
+    void* get(size_t bytes);   // nullptr when no memory is left
+    void put(void* p);
+
+private:
+    struct Block {
+        size_t bytes;
+        bool pinned;
+    };
+    std::multimap<size_t, void*> free_;
+    std::unordered_map<void*, Block> blocks_;
+};
+
+// Keys (each 16-key group contiguous, as readouts emit them) and their amplitudes, in one
+// pooled block: keys, then re, then im.
 struct Run {
-    std::vector<uint64_t> k;
-    std::vector<double> r, i;
+    uint64_t* k = nullptr;
+    double* r = nullptr;
+    double* i = nullptr;
+    uint64_t n = 0;
     uint64_t groups = 0;
     uint64_t all_and = ~0ULL, all_or = 0;
-    void fill_summary();
+
+    Run() = default;
+    Run(const Run&) = delete;
+    Run& operator=(const Run&) = delete;
+    Run(Run&& o) noexcept { take(o); }
+    Run& operator=(Run&& o) noexcept {
+        if (this != &o) {
+            release();
+            take(o);
+        }
+        return *this;
+    }
+    ~Run() { release(); }
+    bool alloc(PinnedPool* pool, uint64_t count);
+    void release();
+    // AND, OR and group count of the keys, on `threads` host threads
+    void fill_summary(int threads);
+
+private:
+    void take(Run& o);
+    PinnedPool* pool_ = nullptr;
+    void* block_ = nullptr;
 };
 
 class PartState {
@@ -57,13 +104,16 @@ private:
     int load_engine(const Run& in);
     int run_windows();
     int run_bin(Run& in, std::vector<sqc_gate> gates, unsigned long long free_bits, std::vector<Run>* out);
+    int distribute(std::vector<Run>& runs, const std::vector<int>& bits, std::vector<Run>* bins);
     uint64_t bin_keys_target() const;
     void take_counters();
     int maybe_return();
 
+    PinnedPool pool_;   // destroyed after the runs that hold its blocks
     Engine eng_;
     uint32_t nq_ = 0;
     double thr_ = 1e-14;
+    int threads_ = 1;
     bool resident_ = true;
     std::vector<Run> runs_;
     std::vector<sqc_gate> pending_;
