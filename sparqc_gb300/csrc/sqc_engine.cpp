@@ -479,6 +479,8 @@ int Engine::rebuild(unsigned long long nb_new) {
     c.list_tail = 0;
     c.empty_groups = 0;
     c.acc_nnz = c.acc_empty = c.acc_upd = 0;
+    c.work = 0;
+    c.units_n = 0;
     std::memcpy(ctl_host_, &c, sizeof c);
     if ((rc = cuda(cudaMemcpyAsync(ctl_, ctl_host_, sizeof(Ctl), cudaMemcpyHostToDevice, stream_), "H2D ctl")))
         return rc;

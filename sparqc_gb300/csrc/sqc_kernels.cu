@@ -53,6 +53,7 @@ __global__ void set_zero_kernel(TableDev t, Ctl* ctl, int dbl) {
         ctl->status = 0;
         ctl->done = 0;
         ctl->work = 0;
+        ctl->units_n = 0;
         ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
         ctl->seq = 0;
         ctl->amp_updates = 0;
@@ -86,6 +87,7 @@ __global__ void set_state_begin_kernel(Ctl* ctl) {
     ctl->status = 0;
     ctl->done = 0;
     ctl->work = 0;
+    ctl->units_n = 0;
     ctl->acc_nnz = ctl->acc_empty = ctl->acc_upd = 0;
     ctl->seq = 0;
     ctl->amp_updates = 0;

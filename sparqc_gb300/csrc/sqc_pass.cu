@@ -70,6 +70,7 @@ __device__ void finish_pass(Ctl* ctl, unsigned long long n, unsigned long long e
         }
         ctl->done = 0;
         ctl->work = 0;
+        ctl->units_n = 0;
         __threadfence();
     }
 }
@@ -138,12 +139,16 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T>::kMin) direct_kernel(Pa
     finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
 }
 
-// ---- resolve: ownership of every unit, before a pass that pairs groups -------------------
-// The list is cut into ranges of R entries (R a multiple of 32, a power of two). One warp per
-// range writes the range's owned units densely at units[r*R ...] (warp ballot, no atomics)
-// and their number to counts[r].
+constexpr int kResolveThreads = 256;
+
+// ---- resolve: the owned units of a pass that pairs groups, before the pass -----------------
+// Every thread settles ownership for one list entry (all lookups of a block in flight at
+// once); each block reserves room for its owned units with one atomic on ctl->units_n and
+// writes them densely, in no particular order. The staged pass deals the units out evenly.
 template <int NX>
-__global__ void __launch_bounds__(256) resolve_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
+    __shared__ unsigned warp_at[kResolveThreads / 32];
+    __shared__ unsigned long long base_sh;
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
@@ -155,29 +160,34 @@ __global__ void __launch_bounds__(256) resolve_kernel(PassArgs a) {
     const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
     const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
     const TableDev t = a.t;
-    const unsigned long long R = a.range;
-    const unsigned long long nranges = (n + R - 1) / R;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    for (unsigned long long r = gw; r < nranges; r += nw) {
-        const unsigned long long e0 = r * R, e1 = umin64(n, e0 + R);
-        unsigned cnt = 0;
-        for (unsigned long long e = e0 + lane; e - lane < e1; e += 32) {
-            Unit u;
-            bool own = false;
-            if (e < e1) {
-                const unsigned b = t.list[e];
-                long long bk[4];
-                own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, bk, &u.G0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (unsigned long long c0 = (unsigned long long)blockIdx.x * kResolveThreads; c0 < n;
+         c0 += (unsigned long long)gridDim.x * kResolveThreads) {
+        const unsigned long long e = c0 + threadIdx.x;
+        Unit u;
+        bool own = false;
+        if (e < n) {
+            const unsigned b = t.list[e];
+            long long bk[4];
+            own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, bk, &u.G0);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
-            }
-            const unsigned om = __ballot_sync(kFull, own);
-            if (own) t.units[e0 + cnt + __popc(om & ((1u << lane) - 1u))] = u;
-            cnt += __popc(om);
+            for (int k = 0; k < 4; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
         }
-        if (lane == 0) t.counts[r] = cnt;
+        const unsigned bal = __ballot_sync(kFull, own);
+        if (lane == 0) warp_at[w] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int i = 0; i < kResolveThreads / 32; ++i) {
+                const unsigned c = warp_at[i];
+                warp_at[i] = tot;
+                tot += c;
+            }
+            base_sh = tot ? atomicAdd(&ctl->units_n, (unsigned long long)tot) : 0ULL;
+        }
+        __syncthreads();
+        if (own) t.units[base_sh + warp_at[w] + __popc(bal & ((1u << lane) - 1u))] = u;
+        __syncthreads();   // warp_at and base_sh are reused by the next chunk
     }
 }
 
@@ -219,68 +229,60 @@ __device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsi
     v.pres0 = v.pres;
 }
 
-// Where a warp's next slot comes from: a strided sequence of 4-entry items (stream pass) or
-// the dense owned pairs of a strided sequence of ranges (pair pass).
-// Items (four list entries, stream passes) and ranges (pair and quad passes) are handed out
-// from the pass's work counter, so the warps finish together.
+// Where a warp's slots come from. The items of a pass -- four list entries (stream pass), two
+// owned pairs (pair pass) or one owned quad (quad pass) -- are dealt out round robin: warp w
+// of W takes items w, w + W, w + 2W, ... Items cost the same, so the warps finish together,
+// and every warp knows its next item in advance: the bucket indices of the item after the one
+// being issued are loaded one issue ahead (lanes 0..3, one bucket each), so no issue waits on
+// them.
 struct SlotSource {
-    unsigned long long next;      // stream: current item; pair/quad: current range
-    unsigned long long u, c;      // pair/quad: next unit within the range, units in the range
-    unsigned long long end;
-    Ctl* ctl;
+    unsigned long long item, stride;   // the next item to load, W
+    unsigned long long count;          // items of the pass
+    unsigned nb;                       // prefetched bucket of this lane (lanes 0..3)
+    unsigned long long ng;             // ... and its group (pair and quad passes)
+    bool nany;                         // the prefetched item exists
 };
 
-__device__ __forceinline__ unsigned long long grab_work(Ctl* ctl, int lane) {
-    unsigned long long w = 0;
-    if (lane == 0) w = atomicAdd(&ctl->work, 1ULL);
-    return shfl64(w, 0);
+template <int NX>
+__device__ __forceinline__ void fetch_item(SlotSource& src, const TableDev& t, unsigned long long n,
+                                           unsigned long long units, unsigned long long m1, unsigned long long m2,
+                                           int lane) {
+    const unsigned long long i = src.item;
+    src.item += src.stride;
+    src.nany = i < src.count;
+    src.nb = kNoBucket;
+    src.ng = 0;
+    if (!src.nany || lane >= 4) return;
+    if (NX == 0) {
+        const unsigned long long e = 4 * i + (unsigned long long)lane;
+        if (e < n) src.nb = t.list[e];
+    } else if (NX == 1) {   // two pairs: buckets (G0, G0|m1) of units 2i and 2i + 1
+        const unsigned long long u = 2 * i + (unsigned long long)(lane >> 1);
+        if (u < units) {
+            const Unit un = t.units[u];
+            src.nb = (lane & 1) ? un.b[1] : un.b[0];
+            src.ng = (lane & 1) ? (un.G0 | m1) : un.G0;
+        }
+    } else {                // one quad: bucket k is member (k & 1, k >> 1)
+        const Unit un = t.units[i];
+        src.nb = lane == 0 ? un.b[0] : lane == 1 ? un.b[1] : lane == 2 ? un.b[2] : un.b[3];
+        src.ng = un.G0 | ((lane & 1) ? m1 : 0ULL) | ((lane & 2) ? m2 : 0ULL);
+    }
 }
 
+// Copy the prefetched item's buckets into a ring slot (cp.async, one commit group) and
+// prefetch the next item.
 template <class T, int NX>
 __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotSource& src, unsigned long long n,
-                                           unsigned long long R, unsigned long long m1, unsigned long long m2,
+                                           unsigned long long units, unsigned long long m1, unsigned long long m2,
                                            int lane) {
     constexpr uint32_t kAmp = (uint32_t)(sizeof(typename AmpT<T>::V) * kSlots);
     constexpr int kKeyChunks = 128 / 16, kAmpChunks = (int)(kAmp / 16);
     constexpr int kChunks = 4 * (kKeyChunks + kAmpChunks) + (NX ? 0 : 4);
-    unsigned bk = kNoBucket;
-    unsigned long long Gk = 0;
-    bool any = false;
-    if (NX == 0) {
-        if (src.next < src.end) src.next = grab_work(src.ctl, lane);
-        if (src.next < src.end) {
-            const unsigned long long e = 4 * src.next + (unsigned long long)lane;
-            if (lane < 4 && e < n) bk = t.list[e];
-            any = true;
-        }
-    } else {
-        while (src.next < src.end && src.u >= src.c) {   // move to the next range with units
-            src.next = grab_work(src.ctl, lane);
-            src.u = 0;
-            src.c = src.next < src.end ? t.counts[src.next] : 0;
-        }
-        if (src.next < src.end) {
-            const unsigned long long base = src.next * R + src.u;
-            if (NX == 1) {   // two pairs: buckets (G0, G0|m1) of units u and u + 1
-                const bool second = src.u + 1 < src.c;
-                const int k = lane & 3;
-                if (lane < 4 && (k < 2 || second)) {
-                    const Unit un = t.units[base + (k >> 1)];
-                    bk = (k & 1) ? un.b[1] : un.b[0];
-                    Gk = (k & 1) ? (un.G0 | m1) : un.G0;
-                }
-                src.u += 2;
-            } else {         // one quad: bucket k is member (k & 1, k >> 1)
-                if (lane < 4) {
-                    const Unit un = t.units[base];
-                    bk = lane == 0 ? un.b[0] : lane == 1 ? un.b[1] : lane == 2 ? un.b[2] : un.b[3];
-                    Gk = un.G0 | ((lane & 1) ? m1 : 0ULL) | ((lane & 2) ? m2 : 0ULL);
-                }
-                src.u += 1;
-            }
-            any = true;
-        }
-    }
+    const unsigned bk = src.nb;
+    const unsigned long long Gk = src.ng;
+    const bool any = src.nany;
+    fetch_item<NX>(src, t, n, units, m1, m2, lane);
     const unsigned b0 = __shfl_sync(kFull, bk, 0), b1 = __shfl_sync(kFull, bk, 1);
     const unsigned b2 = __shfl_sync(kFull, bk, 2), b3 = __shfl_sync(kFull, bk, 3);
     if (lane < 4) {
@@ -329,20 +331,20 @@ __global__ void __launch_bounds__(kStagedThreads) staged_kernel(PassArgs a) {
     const unsigned long long nnz_in = ctl->nnz;
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, jj = lane & 15;
-    const unsigned long long R = a.range;
     const unsigned long long m1 = NX ? 1ULL << (a.q1 - kSlotBits) : 0ULL;
     const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    // owned units, written by this pass's resolve kernel (stream passes: none)
+    const unsigned long long units = NX ? umin64(*(volatile unsigned long long*)&ctl->units_n, n) : 0ULL;
     SlotSource src;
-    src.ctl = ctl;
-    src.next = 0;
-    src.u = 0;
-    src.c = 0;
-    src.end = NX == 0 ? (n + 3) / 4 : (n + R - 1) / R;
+    src.item = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    src.stride = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    src.count = NX == 0 ? (n + 3) / 4 : NX == 1 ? (units + 1) / 2 : units;
+    fetch_item<NX>(src, t, n, units, m1, m2, lane);
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
-    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, R, m1, m2, lane);
+    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, units, m1, m2, lane);
     Val<T> va, vb;
     for (unsigned long long step = 0;; ++step) {
-        issue_slot<T, NX>(ring[(step + kDepth - 1) % kDepth], t, src, n, R, m1, m2, lane);
+        issue_slot<T, NX>(ring[(step + kDepth - 1) % kDepth], t, src, n, units, m1, m2, lane);
         cp_async_wait<kDepth - 1>();
         __syncwarp();
         const Slot<T>& sl = ring[step % kDepth];
@@ -451,11 +453,10 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
     }
     int launched = 0;
     if (nx) {
-        const unsigned long long nranges = list_hint / a.range + 1;
-        const unsigned long long rg = std::min<unsigned long long>((nranges + 7) / 8, (unsigned long long)sms * 8);
-        const int g = (int)std::max<unsigned long long>(rg, 1);
-        if (nx == 1) resolve_kernel<1><<<g, 256, 0, st>>>(a);
-        else resolve_kernel<2><<<g, 256, 0, st>>>(a);
+        const unsigned long long chunks = list_hint / kResolveThreads + 1;
+        const int g = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(chunks, (unsigned long long)sms * 8));
+        if (nx == 1) resolve_kernel<1><<<g, kResolveThreads, 0, st>>>(a);
+        else resolve_kernel<2><<<g, kResolveThreads, 0, st>>>(a);
         ++launched;
     }
     const unsigned long long items = nx == 2 ? list_hint + 1 : nx == 1 ? list_hint / 2 + 1 : (list_hint + 3) / 4;

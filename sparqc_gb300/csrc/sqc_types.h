@@ -69,6 +69,7 @@ struct Ctl {
     double acc[6];                  // reductions: norm, compare
     unsigned long long acc_max;     // bit pattern of a non-negative double (max |a-b|)
     unsigned long long work;        // list entries handed out in the running pass (0 between passes)
+    unsigned long long units_n;     // owned units the running pass's resolve kernel wrote (0 between passes)
 };
 
 // Gate descriptor with host-resolved coefficients (std::cos/std::sin on the host, so the
