@@ -88,7 +88,7 @@ __device__ __forceinline__ void unit_chunk(const TableDev& t, const GateDesc* ga
         long long mb;
         unsigned long long G0;
         const unsigned om = units4<NX>(t, ep, e0, ee, m1, m2, lane, &mb, &G0);
-        run_units4<T, NX, false>(t, ep, ctl, gates, g0, g1, m1, m2, om, mb, G0, lane, pb, va, vb, cnt_nnz, cnt_empty,
+        run_units4<T, NX, false>(t, ep, ctl, gates, nullptr, g0, g1, m1, m2, om, mb, G0, lane, pb, va, vb, cnt_nnz, cnt_empty,
                                  upd);
     }
 }

@@ -24,7 +24,7 @@ struct BPass {
 
 // A circuit of the batch (read-only while the kernel runs).
 struct BCirc {
-    TableDev t;                    // its table slice (units/counts unused)
+    TableDev t;                    // its table slice (units unused)
     const GateDesc* gates;
     const BPass* passes;
     uint32_t npasses;

@@ -193,17 +193,30 @@ __device__ __forceinline__ float ld_desc(const float* p) {
 #endif
 }
 
-// Coefficients are read through a pointer to the (L1-resident, warp-broadcast) descriptor.
+// A gate's (c, s) pair copied to shared memory, with its descriptor for the U matrix.
+template <class T> struct SmemCoef {
+    T c, s;
+    const GateDesc* g;
+};
+
+// Coefficients are read through a pointer to the (L1-resident, warp-broadcast) descriptor, or
+// from the pair a pass staged in shared memory.
 template <class T> struct Coef;
 template <> struct Coef<double> {
     __device__ static __forceinline__ double c(const GateDesc* g) { return ld_desc(&g->c); }
     __device__ static __forceinline__ double s(const GateDesc* g) { return ld_desc(&g->s); }
     __device__ static __forceinline__ double m(const GateDesc* g, int i) { return ld_desc(&g->m[i]); }
+    __device__ static __forceinline__ double c(const SmemCoef<double>& k) { return k.c; }
+    __device__ static __forceinline__ double s(const SmemCoef<double>& k) { return k.s; }
+    __device__ static __forceinline__ double m(const SmemCoef<double>& k, int i) { return ld_desc(&k.g->m[i]); }
 };
 template <> struct Coef<float> {
     __device__ static __forceinline__ float c(const GateDesc* g) { return ld_desc(&g->cf); }
     __device__ static __forceinline__ float s(const GateDesc* g) { return ld_desc(&g->sf); }
     __device__ static __forceinline__ float m(const GateDesc* g, int i) { return ld_desc(&g->mf[i]); }
+    __device__ static __forceinline__ float c(const SmemCoef<float>& k) { return k.c; }
+    __device__ static __forceinline__ float s(const SmemCoef<float>& k) { return k.s; }
+    __device__ static __forceinline__ float m(const SmemCoef<float>& k, int i) { return ld_desc(&k.g->mf[i]); }
 };
 
 // Branching update seen from one member of a pair, for gate kind K: a = own amplitude,
@@ -214,8 +227,8 @@ template <> struct Coef<float> {
 //   Rx: c*own + s*(i-rotated partner)      (symmetric in the two members)
 //   Ry: bit 0 -> c*v0 - s*v1,             bit 1 -> c*v1 + s*v0
 //   U : self term first, then partner term, fused multiply-add chain (no reference form).
-template <class T, uint32_t K>
-__device__ __forceinline__ Cx<T> branch_update(const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ Cx<T> branch_update(const G& g, bool bit, Cx<T> a, Cx<T> b) {
     using A = Arith<T>;
     Cx<T> o;
     if constexpr (K == KH) {
@@ -245,8 +258,8 @@ __device__ __forceinline__ Cx<T> branch_update(const GateDesc* g, bool bit, Cx<T
 }
 
 // Diagonal update of one amplitude for gate kind K (reference: z_core, phase_core, rz_core).
-template <class T, uint32_t K>
-__device__ __forceinline__ Cx<T> diag_update(const GateDesc* g, bool bit, Cx<T> a) {
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ Cx<T> diag_update(const G& g, bool bit, Cx<T> a) {
     using A = Arith<T>;
     if constexpr (K == KZ) return bit ? Cx<T>{neg(a.r), neg(a.i)} : a;
     else if constexpr (K == KS) return bit ? Cx<T>{neg(a.i), a.r} : a;
@@ -274,8 +287,8 @@ __device__ __forceinline__ Cx<T> swap_update(bool bit, Cx<T> b) {
 constexpr uint32_t KANY = 0xFFu;
 
 // Run-time dispatch of the updates (one copy of each kind's code per call site).
-template <class T>
-__device__ __forceinline__ Cx<T> branch_update_rt(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a, Cx<T> b) {
+template <class T, class G>
+__device__ __forceinline__ Cx<T> branch_update_rt(uint32_t kind, const G& g, bool bit, Cx<T> a, Cx<T> b) {
     switch (kind) {
     case KH: return branch_update<T, KH>(g, bit, a, b);
     case KRX: return branch_update<T, KRX>(g, bit, a, b);
@@ -284,8 +297,8 @@ __device__ __forceinline__ Cx<T> branch_update_rt(uint32_t kind, const GateDesc*
     }
 }
 
-template <class T>
-__device__ __forceinline__ Cx<T> diag_update_rt(uint32_t kind, const GateDesc* g, bool bit, Cx<T> a) {
+template <class T, class G>
+__device__ __forceinline__ Cx<T> diag_update_rt(uint32_t kind, const G& g, bool bit, Cx<T> a) {
     switch (kind) {
     case KZ: return diag_update<T, KZ>(g, bit, a);
     case KS: return diag_update<T, KS>(g, bit, a);

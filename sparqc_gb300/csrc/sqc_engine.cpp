@@ -131,7 +131,6 @@ int Engine::alloc_table(unsigned long long nb, HostTable* out) {
         (rc = cuda(cudaMalloc(&t.amps, nb * kSlots * (dbl_ ? 16 : 8)), "cudaMalloc(amps)")) ||
         (rc = cuda(cudaMalloc(&t.list, nb * sizeof(unsigned)), "cudaMalloc(list)")) ||
         (rc = cuda(cudaMalloc(&t.units, nb * sizeof(Unit)), "cudaMalloc(units)")) ||
-        (rc = cuda(cudaMalloc(&t.counts, (nb / 32 + 1) * sizeof(unsigned)), "cudaMalloc(counts)")) ||
         (rc = cuda(cudaMemsetAsync(t.hdr, 0, nb * sizeof(Header), stream_), "cudaMemset(hdr)"))) {
         free_table(&t);
         return rc;
@@ -146,7 +145,6 @@ void Engine::free_table(HostTable* t) {
     if (t->amps) cudaFree(t->amps);
     if (t->list) cudaFree(t->list);
     if (t->units) cudaFree(t->units);
-    if (t->counts) cudaFree(t->counts);
     *t = HostTable();
 }
 
@@ -157,7 +155,6 @@ TableDev Engine::dev() const {
     d.amps = tab_.amps;
     d.list = tab_.list;
     d.units = tab_.units;
-    d.counts = tab_.counts;
     d.mask = tab_.nb - 1;
     return d;
 }
@@ -360,7 +357,6 @@ int Engine::flush() {
         a.grow_bound = group_bound(after[i - 1], nq_);
         if (sp.nx)
             list_hint_ = std::min<unsigned long long>(tab_.nb, std::min(list_hint_ << sp.nx, a.grow_bound));
-        a.range = pass_range(list_hint_, sms_);
         const int nl = launch_pass(a, list_hint_, dbl_, sms_, stream_);
         if (nl < 0) return cuda(cudaGetLastError(), "gate pass");
         const bool pair = sp.nx > 0;
@@ -486,7 +482,6 @@ int Engine::rebuild(unsigned long long nb_new) {
         return rc;
     TableDev nd;
     nd.hdr = nt.hdr; nd.keys = nt.keys; nd.amps = nt.amps; nd.list = nt.list; nd.units = nt.units;
-    nd.counts = nt.counts;
     nd.mask = nt.nb - 1;
     if ((rc = cuda(launch_rehash(dev(), n_old, nd, 1u, dbl_ ? 16 : 8, ctl_, sms_, stream_), "rehash"))) return rc;
     ++launches_;

@@ -21,7 +21,6 @@ struct HostTable {
     void* amps = nullptr;
     unsigned int* list = nullptr;
     Unit* units = nullptr;
-    unsigned int* counts = nullptr;
     unsigned long long nb = 0;
 };
 

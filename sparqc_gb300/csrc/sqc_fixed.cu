@@ -144,7 +144,6 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     t.amps = b + kOffAmps;
     t.list = reinterpret_cast<unsigned*>(b + kOffList);
     t.units = nullptr;    // small tables take the direct pass, which needs neither
-    t.counts = nullptr;
     t.mask = kFixedBuckets - 1;
     Ctl* ctl = reinterpret_cast<Ctl*>(b + kOffCtl);
     GateDesc* d_desc = reinterpret_cast<GateDesc*>(b + kOffDesc);
@@ -184,7 +183,6 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     a.gates = d_desc;
     a.amp_bytes = 16;
     a.max_groups = (unsigned long long)(0.9 * (double)kFixedBuckets);
-    a.range = 32;
     const double thr = 1e-14;
     std::memcpy(&a.prune.d, &thr, sizeof(double));
     float tf = (float)thr;

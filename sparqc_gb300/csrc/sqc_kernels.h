@@ -14,7 +14,6 @@ namespace sqc {
 // Returns the number of kernels launched, or -1 when a launch failed.
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st);
 // List entries per resolve range for a state of about list_hint live buckets.
-unsigned long long pass_range(unsigned long long list_hint, int sms);
 cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st);
 cudaError_t launch_set_state(const unsigned long long* keys, const double* re, const double* im,
                              unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,

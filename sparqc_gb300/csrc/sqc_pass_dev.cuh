@@ -73,8 +73,8 @@ __device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long k
 }
 
 // A branching or swap gate of kind K whose partner slot sits in lane ^ off.
-template <class T, uint32_t K>
-__device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, int off, Val<T>& v,
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off, Val<T>& v,
                                           const PruneBits& pb) {
     const bool sat = slot_sat(h, v.key);
     const bool bit = slot_bit(h, v.key);
@@ -105,8 +105,8 @@ __device__ __forceinline__ void shfl_step(const GateDesc* g, const GateHead& h, 
 }
 
 // A diagonal gate of kind K on one slot (lane-local).
-template <class T, uint32_t K>
-__device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, Val<T>& v) {
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ void diag_step(const G& g, const GateHead& h, Val<T>& v) {
     const bool bit = slot_bit(h, v.key);
     const bool one_sided = K == KANY ? (h.op & kOpOneSided) != 0 : one_sided_kind(K);
     const bool need = v.pres && (!one_sided || bit) && slot_sat(h, v.key);
@@ -119,8 +119,8 @@ __device__ __forceinline__ void diag_step(const GateDesc* g, const GateHead& h, 
 
 // A branching or swap gate of kind K on the pass's first cross-group qubit, lane-local:
 // a = slot of the group with stored target bit 0, b = slot of its partner group.
-template <class T, uint32_t K>
-__device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b,
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>& a, Val<T>& b,
                                           const PruneBits& pb) {
     const bool sat = slot_sat(h, a.key);
     const bool bit_a = (h.op & kOpFlip) != 0, bit_b = !bit_a;
@@ -154,8 +154,8 @@ __device__ __forceinline__ void pair_step(const GateDesc* g, const GateHead& h, 
 }
 
 // One gate of kind K on the lane's two slots, as its pass encoded it (encode_pass).
-template <class T, uint32_t K>
-__device__ __forceinline__ void gate_on(const GateDesc* g, const GateHead& h, Val<T>& a, Val<T>& b,
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ void gate_on(const G& g, const GateHead& h, Val<T>& a, Val<T>& b,
                                         const PruneBits& pb) {
     if constexpr (K == KANY) {   // kind known at run time: category from the encoded op bits
         if (h.op & kOpPair) {
@@ -209,6 +209,87 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
             gate_on<T, KANY>(g, h, a, b, pb);
             continue;
         }
+        switch (h.kind) {
+        case KX: gate_on<T, KX>(g, h, a, b, pb); break;
+        case KY: gate_on<T, KY>(g, h, a, b, pb); break;
+        case KZ: gate_on<T, KZ>(g, h, a, b, pb); break;
+        case KH: gate_on<T, KH>(g, h, a, b, pb); break;
+        case KPHASE: gate_on<T, KPHASE>(g, h, a, b, pb); break;
+        case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
+        case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
+        case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
+        case KS: gate_on<T, KS>(g, h, a, b, pb); break;
+        case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
+        case KT: gate_on<T, KT>(g, h, a, b, pb); break;
+        case KTDG: gate_on<T, KTDG>(g, h, a, b, pb); break;
+        case KU: gate_on<T, KU>(g, h, a, b, pb); break;
+        default: gate_on<T, KYPH>(g, h, a, b, pb); break;
+        }
+    }
+}
+
+// A pass's gate, staged in shared memory by its block: the descriptor's first 32 bytes (kind,
+// target, ctrl, cval, op, credit) and its (c, s) pair in both precisions. Gates are read once
+// per slot held by every warp; from shared memory they never wait on L1 misses.
+struct alignas(16) SmemGate {
+    uint4 h0, h1;
+    double c, s;
+    float cf, sf;
+    uint32_t pad[2];
+};
+
+// Copy gates [g0, g1) (at most kMaxRun) of the pass into shared memory; every thread of the
+// block calls it, and it ends with a barrier.
+__device__ __forceinline__ void stage_gates(SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
+                                            uint32_t g1) {
+    for (uint32_t i = threadIdx.x; g0 + i < g1; i += blockDim.x) {
+        const GateDesc* g = gates + g0 + i;
+        SmemGate x;
+        x.h0 = ld_desc4(g);
+        x.h1 = ld_desc4(reinterpret_cast<const uint4*>(g) + 1);
+        x.c = ld_desc(&g->c);
+        x.s = ld_desc(&g->s);
+        x.cf = ld_desc(&g->cf);
+        x.sf = ld_desc(&g->sf);
+        x.pad[0] = x.pad[1] = 0;
+        sg[i] = x;
+    }
+    __syncthreads();
+}
+
+template <class T> struct SmemPair;
+template <> struct SmemPair<double> {
+    __device__ static __forceinline__ SmemCoef<double> of(const SmemGate& x, const GateDesc* g) {
+        return SmemCoef<double>{x.c, x.s, g};
+    }
+};
+template <> struct SmemPair<float> {
+    __device__ static __forceinline__ SmemCoef<float> of(const SmemGate& x, const GateDesc* g) {
+        return SmemCoef<float>{x.cf, x.sf, g};
+    }
+};
+
+// run_gates with the pass's gates staged in shared memory (sg[i] is gate g0 + i).
+template <class T>
+__device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
+                                            uint32_t g1, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
+                                            unsigned long long& upd) {
+    unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+    bool recount = false;
+    for (uint32_t gi = g0; gi < g1; ++gi) {
+        const SmemGate& x = sg[gi - g0];
+        const uint4 v0 = x.h0, v1 = x.h1;
+        GateHead h;
+        h.kind = v0.x;
+        h.target = v0.y;
+        h.ctrl = (unsigned long long)v0.z | ((unsigned long long)v0.w << 32);
+        h.cval = (unsigned long long)v1.x | ((unsigned long long)v1.y << 32);
+        h.op = v1.z;
+        h.credit = v1.w;
+        const SmemCoef<T> g = SmemPair<T>::of(x, gates + gi);
+        if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        recount = (h.op & kOpBranch) != 0;
+        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
         switch (h.kind) {
         case KX: gate_on<T, KX>(g, h, a, b, pb); break;
         case KY: gate_on<T, KY>(g, h, a, b, pb); break;
@@ -359,9 +440,10 @@ __device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsig
 
 // Process the owned units of a units4 round: pairs two per warp step (one per half), quads one
 // per warp step (the half selects the q2 bit); each unit's groups are loaded straight from the
-// table, the gates applied, and the slots written back.
-template <class T, int NX, bool SPEC = true>
-__device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates, uint32_t g0,
+// table, the gates applied (from shared memory with SMEM), and the slots written back.
+template <class T, int NX, bool SPEC = true, bool SMEM = false>
+__device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates,
+                                           const SmemGate* sg, uint32_t g0,
                                            uint32_t g1, unsigned long long m1, unsigned long long m2, unsigned om,
                                            long long mb, unsigned long long G0,
                                            int lane, const PruneBits& pb, Val<T>& va, Val<T>& vb,
@@ -392,7 +474,8 @@ __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* 
         const bool act = u >= 0;
         load_val_g<T>(t, va, Ga, act ? xa : -1, j);
         load_val_g<T>(t, vb, Ga | m1, act ? xb : -1, j);
-        run_gates<T, SPEC>(gates, g0, g1, va, vb, lane, pb, upd);
+        if constexpr (SMEM) run_gates_s<T>(sg, gates, g0, g1, va, vb, lane, pb, upd);   // gates in shared memory
+        else run_gates<T, SPEC>(gates, g0, g1, va, vb, lane, pb, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         append_new(t, ctl, fa, fb, lane);

@@ -44,8 +44,7 @@ struct TableDev {
     unsigned long long* keys;
     void* amps;
     unsigned int* list;         // live buckets, in claim order
-    Unit* units;                // owned pairs of a pair pass, dense per range of list entries
-    unsigned int* counts;       // owned pairs per range (nb / 32 entries)
+    Unit* units;                // owned units of a pair or quad pass, compacted by the resolve kernel
     unsigned long long mask;    // nb - 1
 };
 
@@ -118,7 +117,6 @@ struct PassArgs {
                             // relabel): each is credited with this pass's input key count
     unsigned long long max_groups;   // a pass that pairs groups refuses to start when its groups
                                      // could exceed this: min(grow_bound, n << nx) > max_groups
-    unsigned long long range;        // list entries per resolve range (power of two, >= 32)
     PruneBits prune;
     uint32_t q1, q2;                 // the cross-group qubits (kNoQubit when absent)
     unsigned long long grow_bound;   // groups the state can hold after the pass, at most
