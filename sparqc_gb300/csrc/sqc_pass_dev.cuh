@@ -238,23 +238,32 @@ struct alignas(16) SmemGate {
     uint32_t pad[2];
 };
 
+// Copy gate g into its shared-memory form.
+__device__ __forceinline__ void stage_gate(SmemGate* d, const GateDesc* g) {
+    SmemGate x;
+    x.h0 = ld_desc4(g);
+    x.h1 = ld_desc4(reinterpret_cast<const uint4*>(g) + 1);
+    x.c = ld_desc(&g->c);
+    x.s = ld_desc(&g->s);
+    x.cf = ld_desc(&g->cf);
+    x.sf = ld_desc(&g->sf);
+    x.pad[0] = x.pad[1] = 0;
+    *d = x;
+}
+
 // Copy gates [g0, g1) (at most kMaxRun) of the pass into shared memory; every thread of the
 // block calls it, and it ends with a barrier.
 __device__ __forceinline__ void stage_gates(SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
                                             uint32_t g1) {
-    for (uint32_t i = threadIdx.x; g0 + i < g1; i += blockDim.x) {
-        const GateDesc* g = gates + g0 + i;
-        SmemGate x;
-        x.h0 = ld_desc4(g);
-        x.h1 = ld_desc4(reinterpret_cast<const uint4*>(g) + 1);
-        x.c = ld_desc(&g->c);
-        x.s = ld_desc(&g->s);
-        x.cf = ld_desc(&g->cf);
-        x.sf = ld_desc(&g->sf);
-        x.pad[0] = x.pad[1] = 0;
-        sg[i] = x;
-    }
+    for (uint32_t i = threadIdx.x; g0 + i < g1; i += blockDim.x) stage_gate(sg + i, gates + g0 + i);
     __syncthreads();
+}
+
+// The same for one warp's own copy (every lane calls it; it ends with a warp barrier).
+__device__ __forceinline__ void stage_gates_warp(SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
+                                                 uint32_t g1, int lane) {
+    for (uint32_t i = (uint32_t)lane; g0 + i < g1; i += 32) stage_gate(sg + i, gates + g0 + i);
+    __syncwarp();
 }
 
 template <class T> struct SmemPair;
@@ -270,7 +279,7 @@ template <> struct SmemPair<float> {
 };
 
 // run_gates with the pass's gates staged in shared memory (sg[i] is gate g0 + i).
-template <class T>
+template <class T, bool SPEC = true>
 __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
                                             uint32_t g1, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
                                             unsigned long long& upd) {
@@ -290,6 +299,10 @@ __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* 
         if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
         recount = (h.op & kOpBranch) != 0;
         if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        if constexpr (!SPEC) {
+            gate_on<T, KANY>(g, h, a, b, pb);
+            continue;
+        }
         switch (h.kind) {
         case KX: gate_on<T, KX>(g, h, a, b, pb); break;
         case KY: gate_on<T, KY>(g, h, a, b, pb); break;
@@ -474,7 +487,7 @@ __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* 
         const bool act = u >= 0;
         load_val_g<T>(t, va, Ga, act ? xa : -1, j);
         load_val_g<T>(t, vb, Ga | m1, act ? xb : -1, j);
-        if constexpr (SMEM) run_gates_s<T>(sg, gates, g0, g1, va, vb, lane, pb, upd);   // gates in shared memory
+        if constexpr (SMEM) run_gates_s<T, SPEC>(sg, gates, g0, g1, va, vb, lane, pb, upd);   // gates in shared memory
         else run_gates<T, SPEC>(gates, g0, g1, va, vb, lane, pb, upd);
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
