@@ -84,7 +84,7 @@ enum { SQC_FP64 = 64, SQC_FP32 = 32 };
 
 typedef struct sqc_options {
     uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 amplitudes */
-    double prune_threshold;    /* default 1e-14: prune iff |re| < thr && |im| < thr (in FP64) */
+    double prune_threshold;    /* > 0, default 1e-14: prune iff |re| < thr && |im| < thr (in FP64) */
     double load_factor;        /* target groups per bucket after growth, default 0.5 */
     uint64_t initial_buckets;  /* initial bucket count (rounded to a power of two), 0 = 1024 */
     void* stream;              /* cudaStream_t to run on; NULL = the handle creates its own */
@@ -232,7 +232,7 @@ typedef struct sqc_batch_options {
     uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 */
     uint32_t device;           /* CUDA device ordinal */
     void* stream;              /* cudaStream_t; NULL = the batch creates its own */
-    double prune_threshold;    /* default 1e-14 */
+    double prune_threshold;    /* > 0, default 1e-14 */
     double load_factor;        /* groups per bucket of a slice at the group bound, (0, 0.45]; default 0.45 */
     uint32_t min_chunk;        /* list entries a warp takes at once, a multiple of 4; default 8 */
     uint32_t blocks_per_sm;    /* persistent blocks per SM, 0 = as many as fit */
@@ -303,7 +303,7 @@ typedef struct sqc_server_options {
     uint32_t precision;        /* SQC_FP64 (default) or SQC_FP32 */
     uint32_t device;
     void* stream;              /* cudaStream_t; NULL = the server creates its own */
-    double prune_threshold;    /* default 1e-14 */
+    double prune_threshold;    /* > 0, default 1e-14 */
     double load_factor;        /* as sqc_batch_options, default 0.45 */
     uint64_t memory_budget;    /* bytes of device memory for slices and gates, 0 = 120 GB (at most 90% of the device) */
     uint32_t max_slots;        /* circuits resident at once, default 1024 */

@@ -121,7 +121,7 @@ int Batch::init(const sqc_batch_options* opt) {
     sqc_batch_default_options(&o);
     if (opt) o = *opt;
     if (o.precision != SQC_FP64 && o.precision != SQC_FP32) return fail(SQC_ERR_ARG, "precision must be 32 or 64");
-    if (!(o.prune_threshold >= 0.0)) return fail(SQC_ERR_ARG, "bad prune threshold");
+    if (!(o.prune_threshold > 0.0)) return fail(SQC_ERR_ARG, "prune_threshold must be > 0");
     if (!(o.load_factor > 0.0 && o.load_factor <= kMaxBatchLoad)) return fail(SQC_ERR_ARG, "load_factor must be in (0, 0.45]");
     if (o.min_chunk == 0 || (o.min_chunk & 3) || o.min_chunk > 4096) return fail(SQC_ERR_ARG, "min_chunk must be a multiple of 4 in 4..4096");
     dbl_ = o.precision == SQC_FP64;

@@ -72,17 +72,24 @@ __device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long k
     return (((unsigned)(key >> h.target) ^ h.op) & 1u) != 0;   // kOpFlip is bit 0
 }
 
-// A branching or swap gate of kind K whose partner slot sits in lane ^ off.
+// Absent slots hold amplitude +-0 (loads zero them, branching updates zero what they prune,
+// swaps move them), and the prune threshold is positive, so a branching update of two absent
+// slots gives a negligible result: "keep iff not negligible" needs no presence test. FP64
+// still forms it, for the warp vote that skips FP64 work no lane needs.
+template <class T> struct NeedAny { static constexpr bool kOn = Vote<T>::kSkip; };
+
+// A branching or swap gate of kind K whose partner slot sits in lane ^ off; bit is the slot's
+// logical target bit.
 template <class T, uint32_t K, class G>
-__device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off, Val<T>& v,
+__device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off, bool bit, Val<T>& v,
                                           const PruneBits& pb) {
     const bool sat = slot_sat(h, v.key);
-    const bool bit = slot_bit(h, v.key);
     Cx<T> pa;
     pa.r = __shfl_xor_sync(kFull, v.amp.r, off);
     pa.i = __shfl_xor_sync(kFull, v.amp.i, off);
-    const bool pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;
     const bool swap = K == KANY ? (h.op & kOpSwap) != 0 : swap_kind(K);
+    bool pp = false;
+    if (swap || NeedAny<T>::kOn) pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;   // warp-uniform
     if (swap) {
         if (sat) {
             v.amp = K == KANY ? swap_update_rt<T>(h.kind, bit, pa) : swap_update<T, K == KANY ? KX : K>(bit, pa);
@@ -90,7 +97,7 @@ __device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off
             v.dirty = true;
         }
     } else {
-        const bool any = v.pres || pp;
+        const bool any = !NeedAny<T>::kOn || v.pres || pp;
         if (warp_needs<T>(sat && any)) {
             const Cx<T> o = K == KANY ? branch_update_rt<T>(h.kind, g, bit, v.amp, pa)
                                       : branch_update<T, K == KANY ? KH : K>(g, bit, v.amp, pa);
@@ -136,7 +143,7 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
             a.dirty = b.dirty = true;
         }
     } else {
-        const bool any = a.pres || b.pres;
+        const bool any = !NeedAny<T>::kOn || a.pres || b.pres;
         if (warp_needs<T>(sat && any)) {
             constexpr uint32_t KB_ = K == KANY ? KH : K;
             const Cx<T> oa = K == KANY ? branch_update_rt<T>(h.kind, g, bit_a, a.amp, b.amp)
@@ -157,13 +164,17 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
 template <class T, uint32_t K, class G>
 __device__ __forceinline__ void gate_on(const G& g, const GateHead& h, Val<T>& a, Val<T>& b,
                                         const PruneBits& pb) {
+    // A shuffled gate targets a qubit below 4 (a bit of the slot index, shared by a and b) or
+    // the quad's second cross-group qubit (whose bit a and b, one unit's groups in one half of
+    // the warp, also share): its target bit is computed once for both slots.
     if constexpr (K == KANY) {   // kind known at run time: category from the encoded op bits
         if (h.op & kOpPair) {
             pair_step<T, KANY>(g, h, a, b, pb);
         } else if (h.op & kOpShfl) {
             const int off = 1 << ((h.op >> kOpOffShift) & 7u);
-            shfl_step<T, KANY>(g, h, off, a, pb);
-            shfl_step<T, KANY>(g, h, off, b, pb);
+            const bool bit = slot_bit(h, a.key);
+            shfl_step<T, KANY>(g, h, off, bit, a, pb);
+            shfl_step<T, KANY>(g, h, off, bit, b, pb);
         } else {
             diag_step<T, KANY>(g, h, a);
             diag_step<T, KANY>(g, h, b);
@@ -173,8 +184,9 @@ __device__ __forceinline__ void gate_on(const G& g, const GateHead& h, Val<T>& a
             pair_step<T, K>(g, h, a, b, pb);
         } else {
             const int off = 1 << ((h.op >> kOpOffShift) & 7u);
-            shfl_step<T, K>(g, h, off, a, pb);
-            shfl_step<T, K>(g, h, off, b, pb);
+            const bool bit = slot_bit(h, a.key);
+            shfl_step<T, K>(g, h, off, bit, a, pb);
+            shfl_step<T, K>(g, h, off, bit, b, pb);
         }
     } else {
         diag_step<T, K>(g, h, a);
