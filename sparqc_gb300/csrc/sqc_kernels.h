@@ -10,10 +10,10 @@
 
 namespace sqc {
 
-// One gate pass (sqc_pass.cu): the resolve kernel (pair passes) and the staged pass kernel.
-// Returns the number of kernels launched, or -1 when a launch failed.
+// One gate pass (sqc_pass.cu): the direct kernel (tables up to 2^20 buckets), or the resolve
+// kernel (pair and quad passes) and the staged kernel. Returns the number of kernels launched,
+// or -1 when a launch failed.
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st);
-// List entries per resolve range for a state of about list_hint live buckets.
 cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st);
 cudaError_t launch_set_state(const unsigned long long* keys, const double* re, const double* im,
                              unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,

@@ -19,7 +19,7 @@
 // the gates and writes the results back in place with ordinary stores. Every
 // pair with at least one present member is read once and written once. A group that appears
 // for the first time is claimed with a 128-bit CAS and appended to the list (such groups are
-// beyond the pass's range). Pruning follows the reference
+// beyond the entries the pass walks). Pruning follows the reference
 // (emulator/device/device_data.cuh:108-156): branching gates drop negligible outputs, swap
 // and diagonal gates keep every key.
 #include "sqc_kernels.h"
