@@ -75,7 +75,7 @@ const char* plan_circuit(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_
     }
     c.end = p;
     split_passes(c.desc.data(), c.desc.size(), max_run, max_nx,
-                 [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, bool fixed) {
+                 [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, uint32_t, bool fixed) {
                      BPass b;
                      std::memset(&b, 0, sizeof b);
                      b.g0 = (uint32_t)g0;

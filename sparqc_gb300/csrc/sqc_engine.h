@@ -107,7 +107,7 @@ private:
     double thr_ = 1e-14;
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
-    uint32_t max_nx_ = 2;        // cross-group qubits per pass at most
+    uint32_t max_nx_ = 2;        // cross-group qubits per pass at most (3: direct-kernel tables only)
     size_t budget_ = 0;
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;

@@ -194,6 +194,7 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
         a.nx = spans[k].pair ? 1u : 0u;
         a.q1 = spans[k].q1;
         a.q2 = kNoQubit;
+        a.q3 = kNoQubit;
         a.grow_bound = ~0ULL;
         a.keys_fixed = spans[k].fixed ? 1u : 0u;
         if (launch_pass(a, kFixedBuckets, true, sms, st) < 0) return SQC_ERR_CUDA;

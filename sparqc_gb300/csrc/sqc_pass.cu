@@ -31,6 +31,8 @@ namespace sqc {
 
 namespace {
 
+constexpr unsigned long long kDirectMaxBuckets = 1ULL << 20;   // larger tables take staged passes
+
 // Block-reduce the pass counters; the last block to finish publishes the pass (key count,
 // list length, empty buckets, pass counter, amp updates, algorithmic bytes). Nothing is
 // published when a pass failed.
@@ -95,10 +97,13 @@ __device__ __forceinline__ bool could_overflow(const PassArgs& a, unsigned long 
 template <class T> struct StagedOcc { static constexpr int kMin = sizeof(T) == 8 ? 6 : 0; };
 template <class T> struct StageGates { static constexpr bool kOn = sizeof(T) == 8; };
 
-template <class T> struct DirectOcc { static constexpr int kMin = sizeof(T) == 8 ? 3 : 4; };
+// Octet passes (three cross-group qubits) hold four slots per lane: FP64 two blocks, FP32 three.
+template <class T, int NX> struct DirectOcc {
+    static constexpr int kMin = NX == 3 ? (sizeof(T) == 8 ? 2 : 3) : (sizeof(T) == 8 ? 3 : 4);
+};
 
 template <class T, int NX>
-__global__ void __launch_bounds__(kThreads, DirectOcc<T>::kMin) direct_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kernel(PassArgs a) {
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
@@ -134,6 +139,17 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T>::kMin) direct_kernel(Pa
             else run_gates<T>(a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
             write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
             write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        }
+    } else if constexpr (NX == 3) {
+        const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
+        const unsigned long long m2 = 1ULL << (a.q2 - kSlotBits);
+        const unsigned long long m3 = 1ULL << (a.q3 - kSlotBits);
+        for (unsigned long long e0 = next4(); e0 < n; e0 = next4()) {
+            long long mb;
+            unsigned long long G0;
+            const unsigned om = units4<3>(t, ep, e0, n, m1, m2, lane, &mb, &G0, m3);
+            run_units8<T, StageGates<T>::kOn>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, m3, om, mb, G0, lane,
+                                              a.prune, cnt_nnz, cnt_empty, upd);
         }
     } else {
         const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
@@ -413,15 +429,17 @@ int staged_residency(bool dbl, int nx) {
 }
 
 int direct_residency(bool dbl, int nx) {
-    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    static int cache[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     int& c = cache[dbl ? 1 : 0][nx];
     if (!c) {
         if (dbl) c = nx == 0 ? occupancy(direct_kernel<double, 0>, kThreads, 0)
                    : nx == 1 ? occupancy(direct_kernel<double, 1>, kThreads, 0)
-                             : occupancy(direct_kernel<double, 2>, kThreads, 0);
+                   : nx == 2 ? occupancy(direct_kernel<double, 2>, kThreads, 0)
+                             : occupancy(direct_kernel<double, 3>, kThreads, 0);
         else c = nx == 0 ? occupancy(direct_kernel<float, 0>, kThreads, 0)
                  : nx == 1 ? occupancy(direct_kernel<float, 1>, kThreads, 0)
-                           : occupancy(direct_kernel<float, 2>, kThreads, 0);
+                 : nx == 2 ? occupancy(direct_kernel<float, 2>, kThreads, 0)
+                           : occupancy(direct_kernel<float, 3>, kThreads, 0);
     }
     return c;
 }
@@ -436,16 +454,17 @@ void launch_staged(const PassArgs& a, int grid, cudaStream_t st) {
     staged_kernel<T, NX><<<grid, kStagedThreads, staged_smem<T>(), st>>>(a);
 }
 
-constexpr unsigned long long kDirectMaxBuckets = 1ULL << 20;
-
 }  // namespace
+
+unsigned long long direct_max_buckets() { return kDirectMaxBuckets; }
 
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
     // list_hint bounds the live-bucket count; grids are sized from it (one resident wave at
     // most); the kernels read the exact count. Tables of up to kDirectMaxBuckets buckets
     // (states that have never needed more) take the direct pass.
     const int nx = (int)a.nx;
-    if (nx < 0 || nx > 2) return -1;
+    if (nx < 0 || nx > 3) return -1;
+    if (nx == 3 && a.t.mask + 1 > kDirectMaxBuckets) return -1;   // octet passes: direct kernel only
     if (a.t.mask + 1 <= kDirectMaxBuckets) {
         const unsigned long long wave = (unsigned long long)sms * direct_residency(dbl, nx);
         const unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
@@ -453,11 +472,13 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
         if (dbl) {
             if (nx == 0) launch_direct<double, 0>(a, grid, st);
             else if (nx == 1) launch_direct<double, 1>(a, grid, st);
-            else launch_direct<double, 2>(a, grid, st);
+            else if (nx == 2) launch_direct<double, 2>(a, grid, st);
+            else launch_direct<double, 3>(a, grid, st);
         } else {
             if (nx == 0) launch_direct<float, 0>(a, grid, st);
             else if (nx == 1) launch_direct<float, 1>(a, grid, st);
-            else launch_direct<float, 2>(a, grid, st);
+            else if (nx == 2) launch_direct<float, 2>(a, grid, st);
+            else launch_direct<float, 3>(a, grid, st);
         }
         return cudaGetLastError() == cudaSuccess ? 1 : -1;
     }

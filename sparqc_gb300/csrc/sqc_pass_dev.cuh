@@ -432,15 +432,15 @@ __device__ __forceinline__ void load_val_g(const TableDev& t, Val<T>& v, unsigne
 }
 
 // Ownership of the units of the (up to) four list entries [e0, e0 + 4) ∩ [0, n) in one round
-// of lookups: with K = 2^NX members per unit, lane l < 4K looks up member k = l % K of the
-// unit of entry l / K. Returns the owner mask (bit e: entry e owns its unit, by unit_owner's
+// of lookups: with K = 2^NX members per unit (NX <= 3, masks m1, m2, m3), lane l < 4K looks up
+// member k = l % K of the unit of entry l / K. Returns the owner mask (bit e: entry e owns its unit, by unit_owner's
 // rule); afterwards lane e*K + k holds member k's bucket (*mb, -1 when absent) and lane e*K
 // the unit's base group (*G0).
 template <int NX>
 __device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsigned long long e0, unsigned long long n,
                                            unsigned long long m1, unsigned long long m2, int lane, long long* mb,
-                                           unsigned long long* G0) {
-    constexpr int K = NX == 2 ? 4 : 2;
+                                           unsigned long long* G0, unsigned long long m3 = 0ULL) {
+    constexpr int K = 1 << NX;
     const int e = lane / K, k = lane % K;
     bool valid = false;
     int idx = 0;
@@ -449,10 +449,12 @@ __device__ __forceinline__ unsigned units4(const TableDev& t, unsigned ep, unsig
     if (lane < 4 * K && e0 + e < n) {
         const long long b = (long long)t.list[e0 + e];
         const unsigned long long G = load_hdr(t.hdr + b).group;
-        idx = ((G & m1) ? 1 : 0) | ((NX == 2 && (G & m2)) ? 2 : 0);
-        *G0 = G & ~(m1 | m2);
+        idx = ((G & m1) ? 1 : 0) | ((NX >= 2 && (G & m2)) ? 2 : 0) | ((NX == 3 && (G & m3)) ? 4 : 0);
+        *G0 = G & ~(m1 | (NX >= 2 ? m2 : 0ULL) | (NX == 3 ? m3 : 0ULL));
         valid = true;
-        *mb = k == idx ? b : lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL));
+        *mb = k == idx ? b
+                       : lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL) |
+                                                 ((k & 4) ? m3 : 0ULL));
     }
     const unsigned live = __ballot_sync(kFull, *mb >= 0);
     const bool own = valid && k == 0 && ((live >> (e * K)) & ((1u << idx) - 1u)) == 0;
@@ -504,6 +506,128 @@ __device__ __forceinline__ void run_units4(const TableDev& t, unsigned ep, Ctl* 
         const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         append_new(t, ctl, fa, fb, lane);
+    }
+}
+
+
+// ---- passes with three cross-group qubits (octets of groups) --------------------------------
+// A unit is the eight groups G0 | i0*m1 | i1*m2 | i2*m3. One warp holds one unit: the half
+// selects i1 (as in a quad), and each lane holds slot j of four groups: a = (0, 0), b = (1, 0),
+// c = (0, 1), d = (1, 1) in (i0, i2). Gates on q1 pair a-b and c-d, gates on q3 pair a-c and
+// b-d (lane-local); gates on q2 and on qubits 0..3 pair lanes (the target bit is shared by the
+// four slots); diagonal gates are lane-local.
+template <class T, uint32_t K, class G>
+__device__ __forceinline__ void gate_on4(const G& g, const GateHead& h, Val<T>& a, Val<T>& b, Val<T>& c, Val<T>& d,
+                                         const PruneBits& pb) {
+    if constexpr (branch_kind(K) || swap_kind(K)) {
+        if (h.op & kOpPair) {
+            pair_step<T, K>(g, h, a, b, pb);
+            pair_step<T, K>(g, h, c, d, pb);
+        } else if (h.op & kOpPair3) {
+            pair_step<T, K>(g, h, a, c, pb);
+            pair_step<T, K>(g, h, b, d, pb);
+        } else {
+            const int off = 1 << ((h.op >> kOpOffShift) & 7u);
+            const bool bit = slot_bit(h, a.key);
+            shfl_step<T, K>(g, h, off, bit, a, pb);
+            shfl_step<T, K>(g, h, off, bit, b, pb);
+            shfl_step<T, K>(g, h, off, bit, c, pb);
+            shfl_step<T, K>(g, h, off, bit, d, pb);
+        }
+    } else {
+        diag_step<T, K>(g, h, a);
+        diag_step<T, K>(g, h, b);
+        diag_step<T, K>(g, h, c);
+        diag_step<T, K>(g, h, d);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ unsigned present4(const Val<T>& a, const Val<T>& b, const Val<T>& c, const Val<T>& d) {
+    return __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres)) +
+           __popc(__ballot_sync(kFull, c.pres)) + __popc(__ballot_sync(kFull, d.pres));
+}
+
+// Gates [g0, g1) on the lane's four slots (from shared memory with SMEM, sg[i] = gate g0 + i).
+template <class T, bool SMEM>
+__device__ __forceinline__ void run_gates4(const SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
+                                           uint32_t g1, Val<T>& a, Val<T>& b, Val<T>& c, Val<T>& d, int lane,
+                                           const PruneBits& pb, unsigned long long& upd) {
+    unsigned n = present4(a, b, c, d);
+    bool recount = false;
+    for (uint32_t gi = g0; gi < g1; ++gi) {
+        GateHead h;
+        if constexpr (SMEM) {
+            const SmemGate& x = sg[gi - g0];
+            const uint4 v0 = x.h0, v1 = x.h1;
+            h.kind = v0.x;
+            h.target = v0.y;
+            h.ctrl = (unsigned long long)v0.z | ((unsigned long long)v0.w << 32);
+            h.cval = (unsigned long long)v1.x | ((unsigned long long)v1.y << 32);
+            h.op = v1.z;
+            h.credit = v1.w;
+        } else {
+            h = gate_head(gates + gi);
+        }
+        if (recount) n = present4(a, b, c, d);
+        recount = (h.op & kOpBranch) != 0;
+        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        auto go = [&](const auto& g) {
+            switch (h.kind) {
+            case KX: gate_on4<T, KX>(g, h, a, b, c, d, pb); break;
+            case KY: gate_on4<T, KY>(g, h, a, b, c, d, pb); break;
+            case KZ: gate_on4<T, KZ>(g, h, a, b, c, d, pb); break;
+            case KH: gate_on4<T, KH>(g, h, a, b, c, d, pb); break;
+            case KPHASE: gate_on4<T, KPHASE>(g, h, a, b, c, d, pb); break;
+            case KRZ: gate_on4<T, KRZ>(g, h, a, b, c, d, pb); break;
+            case KRX: gate_on4<T, KRX>(g, h, a, b, c, d, pb); break;
+            case KRY: gate_on4<T, KRY>(g, h, a, b, c, d, pb); break;
+            case KS: gate_on4<T, KS>(g, h, a, b, c, d, pb); break;
+            case KSDG: gate_on4<T, KSDG>(g, h, a, b, c, d, pb); break;
+            case KT: gate_on4<T, KT>(g, h, a, b, c, d, pb); break;
+            case KTDG: gate_on4<T, KTDG>(g, h, a, b, c, d, pb); break;
+            case KU: gate_on4<T, KU>(g, h, a, b, c, d, pb); break;
+            default: gate_on4<T, KYPH>(g, h, a, b, c, d, pb); break;
+            }
+        };
+        if constexpr (SMEM) go(SmemPair<T>::of(sg[gi - g0], gates + gi));
+        else go(gates + gi);
+    }
+}
+
+// Process the owned octets of a units4<3> round, one per warp step: each half loads its four
+// groups, applies the gates and writes the slots back.
+template <class T, bool SMEM>
+__device__ __forceinline__ void run_units8(const TableDev& t, unsigned ep, Ctl* ctl, const GateDesc* gates,
+                                           const SmemGate* sg, uint32_t g0, uint32_t g1, unsigned long long m1,
+                                           unsigned long long m2, unsigned long long m3, unsigned om, long long mb,
+                                           unsigned long long G0, int lane, const PruneBits& pb,
+                                           unsigned long long& cnt_nnz, unsigned long long& cnt_empty,
+                                           unsigned long long& upd) {
+    constexpr int K = 8;
+    const int half = lane >> 4, j = lane & 15;
+    Val<T> va, vb, vc, vd;
+    while (om) {
+        const int u = __ffs(om) - 1;
+        om &= om - 1;
+        // this half's members: (i0, i1 = half, i2) -> k = i0 + 2*i1 + 4*i2
+        const int ka = 2 * half;
+        const long long xa = (long long)shfl64((unsigned long long)mb, u * K + ka);
+        const long long xb = (long long)shfl64((unsigned long long)mb, u * K + ka + 1);
+        const long long xc = (long long)shfl64((unsigned long long)mb, u * K + ka + 4);
+        const long long xd = (long long)shfl64((unsigned long long)mb, u * K + ka + 5);
+        const unsigned long long Ga = shfl64(G0, u * K) | (half ? m2 : 0ULL);
+        load_val_g<T>(t, va, Ga, xa, j);
+        load_val_g<T>(t, vb, Ga | m1, xb, j);
+        load_val_g<T>(t, vc, Ga | m3, xc, j);
+        load_val_g<T>(t, vd, Ga | m1 | m3, xd, j);
+        run_gates4<T, SMEM>(sg, gates, g0, g1, va, vb, vc, vd, lane, pb, upd);
+        const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+        const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+        const long long fc = write_val<T>(t, ep, vc, lane, &ctl->status, cnt_nnz, cnt_empty);
+        const long long fd = write_val<T>(t, ep, vd, lane, &ctl->status, cnt_nnz, cnt_empty);
+        append_new(t, ctl, fa, fb, lane);
+        append_new(t, ctl, fc, fd, lane);
     }
 }
 

@@ -70,7 +70,7 @@ bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out) {
     return true;
 }
 
-void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1) {
+void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3) {
     for (size_t k = g0; k < g1; ++k) {
         GateDesc& g = d[k];
         uint32_t op = g.flip & kOpFlip;
@@ -83,6 +83,8 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1) {
         if (branch || swap) {
             if (g.target == q1 && g.target >= (uint32_t)kSlotBits) {
                 op |= kOpPair;
+            } else if (g.target == q3 && g.target >= (uint32_t)kSlotBits) {
+                op |= kOpPair3;
             } else {
                 // qubits 0..3: a lane of the same half; the pass's second cross-group qubit:
                 // the other half of the warp

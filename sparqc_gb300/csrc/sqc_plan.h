@@ -46,21 +46,21 @@ bool plan_gate(Planner& p, const sqc_gate& g, GateDesc* out);
 
 // Passes of a descriptor sequence. A pass is a run of at most max_run consecutive gates whose
 // cross-group gates (gates that pair keys of different 16-key groups) target at most
-// max_nx distinct qubits; streamable gates may sit anywhere in it. Passes are cut greedily.
-// f(g0, g1, nx, q1, q2, keys_fixed) is called per pass, q1/q2 the cross-group qubits in order
-// of first use (kNoQubit when absent).
+// max_nx (<= 3) distinct qubits; streamable gates may sit anywhere in it. Passes are cut
+// greedily. f(g0, g1, nx, q1, q2, q3, keys_fixed) is called per pass, q1..q3 the cross-group
+// qubits in order of first use (kNoQubit when absent).
 template <class F>
 void split_passes(const GateDesc* d, size_t n, size_t max_run, uint32_t max_nx, F&& f) {
     size_t i = 0;
     while (i < n) {
         const size_t start = i;
-        uint32_t q[2] = {kNoQubit, kNoQubit};
+        uint32_t q[3] = {kNoQubit, kNoQubit, kNoQubit};
         uint32_t nx = 0;
         while (i < n && i - start < max_run) {
             if (!streamable(d[i])) {
                 const uint32_t t = d[i].target;
-                if (t != q[0] && t != q[1]) {
-                    if (nx >= max_nx) break;
+                if (t != q[0] && t != q[1] && t != q[2]) {
+                    if (nx >= max_nx || nx >= 3) break;
                     q[nx++] = t;
                 }
             }
@@ -68,14 +68,15 @@ void split_passes(const GateDesc* d, size_t n, size_t max_run, uint32_t max_nx, 
         }
         bool fixed = true;
         for (size_t k = start; k < i; ++k) fixed = fixed && is_diag_kind(d[k].kind);
-        f(start, i, nx, q[0], q[1], fixed);
+        f(start, i, nx, q[0], q[1], q[2], fixed);
     }
 }
 
-// Record in descriptors [g0, g1) -- one pass, whose first cross-group qubit is q1 -- how the
-// pass applies each gate (GateDesc.flip kOp* bits). Cross-group gates on another qubit >= 4
-// are on the pass's second cross-group qubit.
-void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1);
+// Record in descriptors [g0, g1) -- one pass with cross-group qubits q1, q2, q3 (in order of
+// first use; kNoQubit when absent) -- how the pass applies each gate (GateDesc.flip kOp*
+// bits): gates on q1 and q3 pair slots held by the same lane, gates on q2 and on qubits 0..3
+// pair lanes (shuffles).
+void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3 = kNoQubit);
 
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose
 // planning ended in p (starting from keys that agreed on every bit of the starting kmask):

@@ -97,6 +97,7 @@ constexpr uint32_t kOpBranch = 1u << 7;    // H, Rx, Ry, U
 constexpr uint32_t kOpSwap = 1u << 8;      // X, Y
 constexpr uint32_t kOpOneSided = 1u << 9;  // diagonal gate that leaves bit-0 keys unchanged
 constexpr uint32_t kOpLowBit = 1u << 10;   // target < 4: the target bit is in the slot index
+constexpr uint32_t kOpPair3 = 1u << 11;    // pairs slots a with c and b with d (third cross-group qubit)
 
 struct PruneBits {
     unsigned long long d;   // bit pattern of thr (double)
@@ -118,7 +119,7 @@ struct PassArgs {
     unsigned long long max_groups;   // a pass that pairs groups refuses to start when its groups
                                      // could exceed this: min(grow_bound, n << nx) > max_groups
     PruneBits prune;
-    uint32_t q1, q2;                 // the cross-group qubits (kNoQubit when absent)
+    uint32_t q1, q2, q3;             // the cross-group qubits (kNoQubit when absent)
     unsigned long long grow_bound;   // groups the state can hold after the pass, at most
 };
 

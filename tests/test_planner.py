@@ -31,12 +31,13 @@ static sqc_gate g(uint32_t kind, uint32_t t, uint64_t ctrl = 0, double th = 0.3)
     return x;
 }
 
-struct P { size_t g0, g1; uint32_t nx, q1, q2; bool fixed; };
+struct P { size_t g0, g1; uint32_t nx, q1, q2, q3; bool fixed; };
 
 static std::vector<P> split(const std::vector<GateDesc>& d, uint32_t max_nx, size_t max_run = 64) {
     std::vector<P> out;
-    split_passes(d.data(), d.size(), max_run, max_nx, [&](size_t a, size_t b, uint32_t nx, uint32_t q1, uint32_t q2, bool f) {
-        out.push_back(P{a, b, nx, q1, q2, f});
+    split_passes(d.data(), d.size(), max_run, max_nx,
+                 [&](size_t a, size_t b, uint32_t nx, uint32_t q1, uint32_t q2, uint32_t q3, bool f) {
+        out.push_back(P{a, b, nx, q1, q2, q3, f});
     });
     return out;
 }
@@ -81,6 +82,19 @@ int main() {
     CHECK(two[1].g0 == 5 && two[1].g1 == 8 && two[1].nx == 1 && two[1].q1 == 7 && two[1].q2 == kNoQubit);
     auto capped = split(s, 2, 2);                       // at most 2 gates per pass
     CHECK(capped.size() == 4);
+    auto three = split(s, 3);                           // qubits 5, 6, 7 in one pass
+    CHECK(three.size() == 1);
+    CHECK(three[0].nx == 3 && three[0].q1 == 5 && three[0].q2 == 6 && three[0].q3 == 7);
+    CHECK(split(s, 4).size() == 1);                     // more than three is three
+    {   // encoding: q1 and q3 pair lane-local slots, q2 and qubits 0..3 shuffle
+        std::vector<GateDesc> e = s;
+        encode_pass(e.data(), 0, e.size(), 5, 7);
+        CHECK((e[0].flip & kOpPair) && !(e[0].flip & kOpPair3));               // H 5
+        CHECK((e[3].flip & kOpShfl) && ((e[3].flip >> kOpOffShift) & 7u) == 4); // Ry 6: other half
+        CHECK((e[5].flip & kOpPair3) && !(e[5].flip & kOpPair));               // Rx 7
+        CHECK((e[2].flip & kOpShfl) && ((e[2].flip >> kOpOffShift) & 7u) == 2); // H 2: lane ^ 4
+        CHECK(!(e[1].flip & (kOpPair | kOpPair3 | kOpShfl)));                 // Z 9: lane-local
+    }
     std::vector<GateDesc> diag;
     for (auto gg : {g(KZ, 30), g(KRZ, 40), g(KT, 2)}) { GateDesc x; CHECK(plan_gate(q, gg, &x)); diag.push_back(x); }
     auto dd = split(diag, 2);
