@@ -93,9 +93,8 @@ typedef struct sqc_options {
     uint32_t time_passes;      /* 1: bracket every gate pass with CUDA events on the handle's stream
                                   (sqc_stats.pass_ns_*); 0 (default): no events */
     uint32_t max_cross_qubits; /* qubits >= 4 one pass may pair keys across (branching or swap gates on
-                                  them), 1, 2 or 3 (3 applies to tables of up to 2^20 buckets; larger
-                                  ones use 2); 0 = default (3 for FP32, 2 for FP64). Results do not
-                                  depend on it. */
+                                  them), 1, 2 or 3; 0 = default (3 for FP32, 2 for FP64). Results do
+                                  not depend on it. */
     uint32_t reserved[2];
 } sqc_options;
 

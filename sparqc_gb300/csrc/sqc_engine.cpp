@@ -340,9 +340,7 @@ int Engine::flush() {
         bool fixed;
     };
     std::vector<Span> spans;
-    // three cross-group qubits per pass only where the passes take the direct kernel
-    const uint32_t max_nx = tab_.nb <= direct_max_buckets() ? max_nx_ : std::min<uint32_t>(max_nx_, 2);
-    split_passes(hd, nd, max_run_, max_nx,
+    split_passes(hd, nd, max_run_, max_nx_,
                  [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, uint32_t q3, bool fixed) {
                      spans.push_back(Span{g0, g1, nx, q1, q2, q3, fixed});
                      encode_pass(hd, g0, g1, q1, q3);

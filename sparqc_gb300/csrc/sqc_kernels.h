@@ -14,9 +14,6 @@ namespace sqc {
 // kernel (pair and quad passes) and the staged kernel. Returns the number of kernels launched,
 // or -1 when a launch failed.
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st);
-// Largest table (buckets) whose passes take the direct kernel; only those may pair across three
-// cross-group qubits.
-unsigned long long direct_max_buckets();
 cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st);
 cudaError_t launch_set_state(const unsigned long long* keys, const double* re, const double* im,
                              unsigned long long n, const TableDev& t, Ctl* ctl, bool dbl, int sms,

@@ -94,7 +94,9 @@ __device__ __forceinline__ bool could_overflow(const PassArgs& a, unsigned long 
 // on large tables), FP32 passes through L1 (the staging's registers cost FP32 more than it
 // saves). Blocks per SM the staged kernel's registers are sized for: FP64 six; FP32 left to the
 // compiler (0: no minimum).
-template <class T> struct StagedOcc { static constexpr int kMin = sizeof(T) == 8 ? 6 : 0; };
+template <class T, int NX> struct StagedOcc {
+    static constexpr int kMin = sizeof(T) == 8 ? (NX == 3 ? 4 : 6) : 0;   // FP64 octets: 53 KB rings, four blocks
+};
 template <class T> struct StageGates { static constexpr bool kOn = sizeof(T) == 8; };
 
 // Octet passes (three cross-group qubits) hold four slots per lane: FP64 two blocks, FP32 three.
@@ -184,7 +186,8 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
     }
     const unsigned ep = ctl->epoch;
     const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
-    const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    const unsigned long long m2 = NX >= 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    const unsigned long long m3 = NX == 3 ? 1ULL << (a.q3 - kSlotBits) : 0ULL;
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (unsigned long long c0 = (unsigned long long)blockIdx.x * kResolveThreads; c0 < n;
@@ -194,10 +197,10 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
         bool own = false;
         if (e < n) {
             const unsigned b = t.list[e];
-            long long bk[4];
-            own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, bk, &u.G0);
+            long long bk[8];
+            own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, m3, bk, &u.G0);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
+            for (int k = 0; k < 8; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
         }
         const unsigned bal = __ballot_sync(kFull, own);
         if (lane == 0) warp_at[w] = __popc(bal);
@@ -227,18 +230,20 @@ constexpr int kWarpsPerBlock = 4;
 constexpr int kStagedThreads = 32 * kWarpsPerBlock;
 constexpr int kDepth = 4;
 
-template <class T> struct Slot {
-    unsigned long long keys[4][kSlots];
-    typename AmpT<T>::V amps[4][kSlots];
-    Header hdr[4];              // stream passes: copied headers (groups)
-    unsigned long long G[4];    // pair passes: group of each held bucket
-    unsigned int b[4];          // bucket index, kNoBucket when absent
+// A ring slot: the buckets of one item, NB = 4 (stream, pair and quad passes) or 8 (octets).
+template <class T, int NB> struct Slot {
+    unsigned long long keys[NB][kSlots];
+    typename AmpT<T>::V amps[NB][kSlots];
+    Header hdr[NB];             // stream passes: copied headers (groups)
+    unsigned long long G[NB];   // pair passes: group of each held bucket
+    unsigned int b[NB];         // bucket index, kNoBucket when absent
     int n;                      // 0: nothing more for this warp
     int pad[3];
 };
+template <int NX> struct SlotBuckets { static constexpr int kN = NX == 3 ? 8 : 4; };
 
-template <class T>
-__device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsigned b, const Slot<T>& sl, int k,
+template <class T, int NB>
+__device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsigned b, const Slot<T, NB>& sl, int k,
                                            int j) {
     v.key = (G << kSlotBits) | (unsigned long long)j;
     v.b = b == kNoBucket ? -1 : (long long)b;
@@ -256,29 +261,29 @@ __device__ __forceinline__ void load_val_s(Val<T>& v, unsigned long long G, unsi
 }
 
 // Where a warp's slots come from. The items of a pass -- four list entries (stream pass), two
-// owned pairs (pair pass) or one owned quad (quad pass) -- are dealt out round robin: warp w
-// of W takes items w, w + W, w + 2W, ... Items cost the same, so the warps finish together,
+// owned pairs (pair pass), one owned quad or one owned octet -- are dealt out round robin: warp
+// w of W takes items w, w + W, w + 2W, ... Items cost the same, so the warps finish together,
 // and every warp knows its next item in advance: the bucket indices of the item after the one
-// being issued are loaded one issue ahead (lanes 0..3, one bucket each), so no issue waits on
-// them.
+// being issued are loaded one issue ahead (lanes 0..NB-1, one bucket each), so no issue waits
+// on them.
 struct SlotSource {
     unsigned long long item, stride;   // the next item to load, W
     unsigned long long count;          // items of the pass
-    unsigned nb;                       // prefetched bucket of this lane (lanes 0..3)
-    unsigned long long ng;             // ... and its group (pair and quad passes)
+    unsigned nb;                       // prefetched bucket of this lane (lanes 0..NB-1)
+    unsigned long long ng;             // ... and its group (pair, quad and octet passes)
     bool nany;                         // the prefetched item exists
 };
 
 template <int NX>
 __device__ __forceinline__ void fetch_item(SlotSource& src, const TableDev& t, unsigned long long n,
                                            unsigned long long units, unsigned long long m1, unsigned long long m2,
-                                           int lane) {
+                                           unsigned long long m3, int lane) {
     const unsigned long long i = src.item;
     src.item += src.stride;
     src.nany = i < src.count;
     src.nb = kNoBucket;
     src.ng = 0;
-    if (!src.nany || lane >= 4) return;
+    if (!src.nany || lane >= SlotBuckets<NX>::kN) return;
     if (NX == 0) {
         const unsigned long long e = 4 * i + (unsigned long long)lane;
         if (e < n) src.nb = t.list[e];
@@ -289,29 +294,34 @@ __device__ __forceinline__ void fetch_item(SlotSource& src, const TableDev& t, u
             src.nb = (lane & 1) ? un.b[1] : un.b[0];
             src.ng = (lane & 1) ? (un.G0 | m1) : un.G0;
         }
-    } else {                // one quad: bucket k is member (k & 1, k >> 1)
-        const Unit un = t.units[i];
-        src.nb = lane == 0 ? un.b[0] : lane == 1 ? un.b[1] : lane == 2 ? un.b[2] : un.b[3];
-        src.ng = un.G0 | ((lane & 1) ? m1 : 0ULL) | ((lane & 2) ? m2 : 0ULL);
+    } else {                // one quad or octet: bucket k is member k = i0 + 2*i1 + 4*i2
+        src.nb = t.units[i].b[lane];
+        src.ng = t.units[i].G0 | ((lane & 1) ? m1 : 0ULL) | ((lane & 2) ? m2 : 0ULL) | ((lane & 4) ? m3 : 0ULL);
     }
 }
 
 // Copy the prefetched item's buckets into a ring slot (cp.async, one commit group) and
 // prefetch the next item.
 template <class T, int NX>
-__device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotSource& src, unsigned long long n,
-                                           unsigned long long units, unsigned long long m1, unsigned long long m2,
-                                           int lane) {
+__device__ __forceinline__ void issue_slot(Slot<T, SlotBuckets<NX>::kN>& sl, const TableDev& t, SlotSource& src,
+                                           unsigned long long n, unsigned long long units, unsigned long long m1,
+                                           unsigned long long m2, unsigned long long m3, int lane) {
+    constexpr int NB = SlotBuckets<NX>::kN;
     constexpr uint32_t kAmp = (uint32_t)(sizeof(typename AmpT<T>::V) * kSlots);
     constexpr int kKeyChunks = 128 / 16, kAmpChunks = (int)(kAmp / 16);
-    constexpr int kChunks = 4 * (kKeyChunks + kAmpChunks) + (NX ? 0 : 4);
+    constexpr int kChunks = NB * (kKeyChunks + kAmpChunks) + (NX ? 0 : 4);
     const unsigned bk = src.nb;
     const unsigned long long Gk = src.ng;
     const bool any = src.nany;
-    fetch_item<NX>(src, t, n, units, m1, m2, lane);
+    fetch_item<NX>(src, t, n, units, m1, m2, m3, lane);
     const unsigned b0 = __shfl_sync(kFull, bk, 0), b1 = __shfl_sync(kFull, bk, 1);
     const unsigned b2 = __shfl_sync(kFull, bk, 2), b3 = __shfl_sync(kFull, bk, 3);
-    if (lane < 4) {
+    unsigned b4 = kNoBucket, b5 = kNoBucket, b6 = kNoBucket, b7 = kNoBucket;
+    if constexpr (NB == 8) {
+        b4 = __shfl_sync(kFull, bk, 4); b5 = __shfl_sync(kFull, bk, 5);
+        b6 = __shfl_sync(kFull, bk, 6); b7 = __shfl_sync(kFull, bk, 7);
+    }
+    if (lane < NB) {
         sl.b[lane] = bk;
         sl.G[lane] = Gk;
     }
@@ -320,20 +330,21 @@ __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotS
         int k, off;
         const char* s;
         char* d;
-        if (c < 4 * kKeyChunks) {
+        if (c < NB * kKeyChunks) {
             k = c / kKeyChunks; off = (c % kKeyChunks) * 16;
-        } else if (c < 4 * (kKeyChunks + kAmpChunks)) {
-            const int x = c - 4 * kKeyChunks;
+        } else if (c < NB * (kKeyChunks + kAmpChunks)) {
+            const int x = c - NB * kKeyChunks;
             k = x / kAmpChunks; off = (x % kAmpChunks) * 16;
         } else {
-            k = c - 4 * (kKeyChunks + kAmpChunks); off = 0;
+            k = c - NB * (kKeyChunks + kAmpChunks); off = 0;
         }
-        const unsigned b = k == 0 ? b0 : k == 1 ? b1 : k == 2 ? b2 : b3;
+        const unsigned b = k < 4 ? (k == 0 ? b0 : k == 1 ? b1 : k == 2 ? b2 : b3)
+                                 : (k == 4 ? b4 : k == 5 ? b5 : k == 6 ? b6 : b7);
         if (b == kNoBucket) continue;
-        if (c < 4 * kKeyChunks) {
+        if (c < NB * kKeyChunks) {
             s = reinterpret_cast<const char*>(t.keys + (size_t)b * kSlots) + off;
             d = reinterpret_cast<char*>(sl.keys[k]) + off;
-        } else if (c < 4 * (kKeyChunks + kAmpChunks)) {
+        } else if (c < NB * (kKeyChunks + kAmpChunks)) {
             s = reinterpret_cast<const char*>(t.amps) + (size_t)b * kAmp + off;
             d = reinterpret_cast<char*>(sl.amps[k]) + off;
         } else {
@@ -347,9 +358,10 @@ __device__ __forceinline__ void issue_slot(Slot<T>& sl, const TableDev& t, SlotS
 
 
 template <class T, int NX>
-__global__ void __launch_bounds__(kStagedThreads, StagedOcc<T>::kMin) staged_kernel(PassArgs a) {
+__global__ void __launch_bounds__(kStagedThreads, StagedOcc<T, NX>::kMin) staged_kernel(PassArgs a) {
+    constexpr int NB = SlotBuckets<NX>::kN;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    Slot<T>* ring = reinterpret_cast<Slot<T>*>(smem_raw) + (threadIdx.x >> 5) * kDepth;
+    Slot<T, NB>* ring = reinterpret_cast<Slot<T, NB>*>(smem_raw) + (threadIdx.x >> 5) * kDepth;
     __shared__ SmemGate sg[StageGates<T>::kOn ? kMaxRun : 1];
 
     Ctl* ctl = a.ctl;
@@ -361,23 +373,41 @@ __global__ void __launch_bounds__(kStagedThreads, StagedOcc<T>::kMin) staged_ker
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, jj = lane & 15;
     const unsigned long long m1 = NX ? 1ULL << (a.q1 - kSlotBits) : 0ULL;
-    const unsigned long long m2 = NX == 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    const unsigned long long m2 = NX >= 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
+    const unsigned long long m3 = NX == 3 ? 1ULL << (a.q3 - kSlotBits) : 0ULL;
     // owned units, written by this pass's resolve kernel (stream passes: none)
     const unsigned long long units = NX ? umin64(*(volatile unsigned long long*)&ctl->units_n, n) : 0ULL;
     SlotSource src;
     src.item = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     src.stride = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
     src.count = NX == 0 ? (n + 3) / 4 : NX == 1 ? (units + 1) / 2 : units;
-    fetch_item<NX>(src, t, n, units, m1, m2, lane);
+    fetch_item<NX>(src, t, n, units, m1, m2, m3, lane);
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
-    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, units, m1, m2, lane);
+    for (int d = 0; d < kDepth - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, units, m1, m2, m3, lane);
     Val<T> va, vb;
     for (unsigned long long step = 0;; ++step) {
-        issue_slot<T, NX>(ring[(step + kDepth - 1) % kDepth], t, src, n, units, m1, m2, lane);
+        issue_slot<T, NX>(ring[(step + kDepth - 1) % kDepth], t, src, n, units, m1, m2, m3, lane);
         cp_async_wait<kDepth - 1>();
         __syncwarp();
-        const Slot<T>& sl = ring[step % kDepth];
+        const Slot<T, NB>& sl = ring[step % kDepth];
         if (sl.n == 0) break;
+        if constexpr (NX == 3) {   // one octet: this half's members (i0, half, i2), four slots per lane
+            const int k0 = 2 * half;
+            Val<T> vc, vd;
+            load_val_s<T>(va, sl.G[k0], sl.b[k0], sl, k0, jj);
+            load_val_s<T>(vb, sl.G[k0 + 1], sl.b[k0 + 1], sl, k0 + 1, jj);
+            load_val_s<T>(vc, sl.G[k0 + 4], sl.b[k0 + 4], sl, k0 + 4, jj);
+            load_val_s<T>(vd, sl.G[k0 + 5], sl.b[k0 + 5], sl, k0 + 5, jj);
+            __syncwarp();
+            run_gates4<T, StageGates<T>::kOn>(sg, a.gates, a.g0, a.g1, va, vb, vc, vd, lane, a.prune, upd);
+            const long long fa = write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
+            const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
+            const long long fc = write_val<T>(t, ep, vc, lane, &ctl->status, cnt_nnz, cnt_empty);
+            const long long fd = write_val<T>(t, ep, vd, lane, &ctl->status, cnt_nnz, cnt_empty);
+            append_new(t, ctl, fa, fb, lane);
+            append_new(t, ctl, fc, fd, lane);
+            continue;
+        }
         const int ka = 2 * half, kb = ka + 1;
         const unsigned ba = sl.b[ka], bb = sl.b[kb];
         unsigned long long Ga, Gb;
@@ -401,9 +431,9 @@ __global__ void __launch_bounds__(kStagedThreads, StagedOcc<T>::kMin) staged_ker
     finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
 }
 
-template <class T>
+template <class T, int NX>
 constexpr size_t staged_smem() {
-    return (size_t)kWarpsPerBlock * kDepth * sizeof(Slot<T>);
+    return (size_t)kWarpsPerBlock * kDepth * sizeof(Slot<T, SlotBuckets<NX>::kN>);
 }
 
 template <class K>
@@ -414,16 +444,24 @@ int occupancy(K kernel, int threads, size_t smem) {
 }
 
 // Resident blocks per SM of each staged-kernel instantiation (queried once per process).
+// Occupancy of one staged-kernel instantiation; rings above the 48 KB default (FP64 octets)
+// are allowed first.
+template <class T, int NX>
+int staged_occupancy() {
+    if (staged_smem<T, NX>() > (48u << 10))
+        cudaFuncSetAttribute(staged_kernel<T, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)staged_smem<T, NX>());
+    return occupancy(staged_kernel<T, NX>, kStagedThreads, staged_smem<T, NX>());
+}
+
 int staged_residency(bool dbl, int nx) {
-    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    static int cache[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     int& c = cache[dbl ? 1 : 0][nx];
     if (!c) {
-        if (dbl) c = nx == 0 ? occupancy(staged_kernel<double, 0>, kStagedThreads, staged_smem<double>())
-                   : nx == 1 ? occupancy(staged_kernel<double, 1>, kStagedThreads, staged_smem<double>())
-                             : occupancy(staged_kernel<double, 2>, kStagedThreads, staged_smem<double>());
-        else c = nx == 0 ? occupancy(staged_kernel<float, 0>, kStagedThreads, staged_smem<float>())
-                 : nx == 1 ? occupancy(staged_kernel<float, 1>, kStagedThreads, staged_smem<float>())
-                           : occupancy(staged_kernel<float, 2>, kStagedThreads, staged_smem<float>());
+        if (dbl) c = nx == 0 ? staged_occupancy<double, 0>() : nx == 1 ? staged_occupancy<double, 1>()
+                   : nx == 2 ? staged_occupancy<double, 2>() : staged_occupancy<double, 3>();
+        else c = nx == 0 ? staged_occupancy<float, 0>() : nx == 1 ? staged_occupancy<float, 1>()
+                 : nx == 2 ? staged_occupancy<float, 2>() : staged_occupancy<float, 3>();
     }
     return c;
 }
@@ -451,12 +489,10 @@ void launch_direct(const PassArgs& a, int grid, cudaStream_t st) {
 
 template <class T, int NX>
 void launch_staged(const PassArgs& a, int grid, cudaStream_t st) {
-    staged_kernel<T, NX><<<grid, kStagedThreads, staged_smem<T>(), st>>>(a);
+    staged_kernel<T, NX><<<grid, kStagedThreads, staged_smem<T, NX>(), st>>>(a);
 }
 
 }  // namespace
-
-unsigned long long direct_max_buckets() { return kDirectMaxBuckets; }
 
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
     // list_hint bounds the live-bucket count; grids are sized from it (one resident wave at
@@ -464,7 +500,6 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
     // (states that have never needed more) take the direct pass.
     const int nx = (int)a.nx;
     if (nx < 0 || nx > 3) return -1;
-    if (nx == 3 && a.t.mask + 1 > kDirectMaxBuckets) return -1;   // octet passes: direct kernel only
     if (a.t.mask + 1 <= kDirectMaxBuckets) {
         const unsigned long long wave = (unsigned long long)sms * direct_residency(dbl, nx);
         const unsigned long long g = (list_hint / 4 + 1 + kThreads / 32 - 1) / (kThreads / 32);
@@ -487,20 +522,23 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
         const unsigned long long chunks = list_hint / kResolveThreads + 1;
         const int g = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(chunks, (unsigned long long)sms * 8));
         if (nx == 1) resolve_kernel<1><<<g, kResolveThreads, 0, st>>>(a);
-        else resolve_kernel<2><<<g, kResolveThreads, 0, st>>>(a);
+        else if (nx == 2) resolve_kernel<2><<<g, kResolveThreads, 0, st>>>(a);
+        else resolve_kernel<3><<<g, kResolveThreads, 0, st>>>(a);
         ++launched;
     }
-    const unsigned long long items = nx == 2 ? list_hint + 1 : nx == 1 ? list_hint / 2 + 1 : (list_hint + 3) / 4;
+    const unsigned long long items = nx >= 2 ? list_hint + 1 : nx == 1 ? list_hint / 2 + 1 : (list_hint + 3) / 4;
     const unsigned long long wave = (unsigned long long)sms * staged_residency(dbl, nx);
     const int grid = (int)std::max<unsigned long long>(1, std::min(wave, (items + 3) / 4));
     if (dbl) {
         if (nx == 0) launch_staged<double, 0>(a, grid, st);
         else if (nx == 1) launch_staged<double, 1>(a, grid, st);
-        else launch_staged<double, 2>(a, grid, st);
+        else if (nx == 2) launch_staged<double, 2>(a, grid, st);
+        else launch_staged<double, 3>(a, grid, st);
     } else {
         if (nx == 0) launch_staged<float, 0>(a, grid, st);
         else if (nx == 1) launch_staged<float, 1>(a, grid, st);
-        else launch_staged<float, 2>(a, grid, st);
+        else if (nx == 2) launch_staged<float, 2>(a, grid, st);
+        else launch_staged<float, 3>(a, grid, st);
     }
     ++launched;
     return cudaGetLastError() == cudaSuccess ? launched : -1;

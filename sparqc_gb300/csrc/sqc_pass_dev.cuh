@@ -335,28 +335,30 @@ __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* 
 }
 
 // Ownership of the unit of list entry group G (bucket b) in a pass with nx cross-group qubits
-// (masks m1, m2): the unit's members are G0 | i0*m1 | i1*m2 (G0 = G with those bits cleared);
-// the owner is the member with the smallest index i0 + 2*i1 among those live at the start of
-// the pass -- for a pair this is the reference's rule (the bit-0 key owns the pair unless it
+// (masks m1, m2, m3): the unit's members are G0 | i0*m1 | i1*m2 | i2*m3 (G0 = G with those bits
+// cleared); the owner is the member with the smallest index i0 + 2*i1 + 4*i2 among those live at
+// the start of the pass -- for a pair this is the reference's rule (the bit-0 key owns the pair unless it
 // is absent, emulator/device/device_table_FC.cuh:62-110) lifted to groups. Fills the members'
 // buckets (-1 when absent) and returns whether G owns its unit. Members a pass creates are
 // only ever created by the unit's owner, after its own check, so the lookups are consistent.
 template <int NX>
 __device__ __forceinline__ bool unit_owner(const TableDev& t, unsigned ep, unsigned long long G, long long b,
-                                           unsigned long long m1, unsigned long long m2, long long bk[4],
-                                           unsigned long long* G0) {
-    constexpr int K = NX == 2 ? 4 : 2;
-    const int idx = ((G & m1) ? 1 : 0) | ((NX == 2 && (G & m2)) ? 2 : 0);
-    *G0 = G & ~(m1 | (NX == 2 ? m2 : 0ULL));
-    bk[0] = bk[1] = bk[2] = bk[3] = -1;
+                                           unsigned long long m1, unsigned long long m2, unsigned long long m3,
+                                           long long bk[8], unsigned long long* G0) {
+    constexpr int K = 1 << NX;
+    const int idx = ((G & m1) ? 1 : 0) | ((NX >= 2 && (G & m2)) ? 2 : 0) | ((NX == 3 && (G & m3)) ? 4 : 0);
+    *G0 = G & ~(m1 | (NX >= 2 ? m2 : 0ULL) | (NX == 3 ? m3 : 0ULL));
+    auto member = [&](int k) { return *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL) | ((k & 4) ? m3 : 0ULL); };
+#pragma unroll
+    for (int k = 0; k < 8; ++k) bk[k] = -1;
 #pragma unroll
     for (int k = 0; k < K; ++k) {   // a live member of smaller index owns the unit
-        if (k < idx && lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL)) >= 0) return false;
+        if (k < idx && lookup_group(t, ep, member(k)) >= 0) return false;
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if (k == idx) bk[k] = b;
-        else if (k > idx) bk[k] = lookup_group(t, ep, *G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL));
+        else if (k > idx) bk[k] = lookup_group(t, ep, member(k));
     }
     return true;
 }

@@ -30,13 +30,14 @@ struct alignas(16) Header {
 };
 
 // One unit of a pass that pairs groups, resolved before the pass. With cross-group qubits
-// q1 (mask m1 = 1 << (q1 - 4)) and, for a quad pass, q2 (m2), the unit is the set of groups
-// G0 | i0*m1 | i1*m2 with G0 having both stored bits 0; b[i0 + 2*i1] is the bucket of member
-// (i0, i1), kNoBucket when the group is absent. Pair passes use b[0], b[1].
+// q1, q2, q3 (masks m1 = 1 << (q1 - 4), ...; a pair pass has q1 only, a quad pass q1 and q2),
+// the unit is the set of groups G0 | i0*m1 | i1*m2 | i2*m3 with G0 having those stored bits 0;
+// b[i0 + 2*i1 + 4*i2] is the bucket of member (i0, i1, i2), kNoBucket when the group is absent.
+// Pair passes use b[0..1], quad passes b[0..3], octet passes b[0..7].
 constexpr unsigned kNoBucket = 0xFFFFFFFFu;
 struct alignas(16) Unit {
     unsigned long long G0;
-    unsigned int b[4];
+    unsigned int b[8];
 };
 
 struct TableDev {

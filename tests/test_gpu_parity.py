@@ -74,8 +74,7 @@ def test_random_circuits_bitexact_staged_path(seed, precision):
 @pytest.mark.parametrize("precision", [64, 32])
 def test_pair_and_quad_passes_agree(buckets, precision):
     """Passes pairing across one, two or three high qubits give the same bits as each other and
-    as the oracle, on the direct (small table) and the staged (large table) kernels; three
-    applies to direct-kernel tables only (larger ones fall back to two)."""
+    as the oracle, on the direct (small table) and the staged (large table) kernels."""
     rng = circuits.SplitMix64(circuits.stream_seed("quad", buckets, precision))
     g = circuits.random_circuit(36, 11, 400, 2, rng, kinds=ALL_KINDS)
     got1, s1 = run_gpu(36, g, precision, initial_buckets=buckets, max_cross_qubits=1)
@@ -86,22 +85,19 @@ def test_pair_and_quad_passes_agree(buckets, precision):
     assert_identical(got2, want)
     assert_identical(got3, want)
     assert s1["amp_updates"] == s2["amp_updates"] == s3["amp_updates"] == upd
-    assert s2["passes"] < s1["passes"]
-    if buckets < STAGED_BUCKETS:
-        assert s3["passes"] < s2["passes"]
-    else:
-        assert s3["passes"] == s2["passes"]
+    assert s3["passes"] < s2["passes"] < s1["passes"]
 
 
+@pytest.mark.parametrize("buckets", [64, STAGED_BUCKETS])
 @pytest.mark.parametrize("seed", range(4))
 @pytest.mark.parametrize("precision", [64, 32])
-def test_octet_passes_bitexact(seed, precision):
+def test_octet_passes_bitexact(seed, precision, buckets):
     """Passes over three high qubits (eight groups per unit, four slots per lane) against the
-    oracle, with every gate kind, controls and growth."""
+    oracle, with every gate kind, controls and growth, on the direct and the staged kernels."""
     rng = circuits.SplitMix64(circuits.stream_seed("octet", seed, precision))
     nq = (14, 24, 40, 64)[seed]
     g = circuits.random_circuit(nq, min(nq, 9 + 2 * seed), 300, 3, rng, kinds=ALL_KINDS)
-    got, stats = run_gpu(nq, g, precision, initial_buckets=64, max_cross_qubits=3)
+    got, stats = run_gpu(nq, g, precision, initial_buckets=buckets, max_cross_qubits=3)
     want, upd = run_oracle(g, precision)
     assert_identical(got, want)
     assert stats["amp_updates"] == upd
