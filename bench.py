@@ -232,6 +232,13 @@ def profile_for(args, staged):
     return f"{'staged' if staged else 'direct'}_kernel_{args.workload}_{prec}"
 
 
+def pinned(n, dtype):
+    """A page-locked host array of n elements (torch's pinned allocator, viewed as numpy)."""
+    import torch
+    tdt = {np.uint64: torch.int64, np.float64: torch.float64}[dtype]
+    return torch.empty(n, dtype=tdt, pin_memory=True).numpy().view(dtype)
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -331,10 +338,11 @@ def run_gpu(args):
         t_max = t_dev
     value = upd_per_step * args.steps * world / t_max
 
-    # e2e: through the C ABI with host buffers (gate array in, final state out)
-    keys = np.empty(1 << p["k"], np.uint64)
-    re = np.empty_like(keys, dtype=np.float64)
-    im = np.empty_like(keys, dtype=np.float64)
+    # e2e: through the C ABI with host buffers (gate array in, final state out into page-locked
+    # host arrays)
+    keys = pinned(1 << p["k"], np.uint64)
+    re = pinned(1 << p["k"], np.float64)
+    im = pinned(1 << p["k"], np.float64)
     got = engine.ctypes.c_uint64()
     L = engine.load()
     gates_c = np.ascontiguousarray(gates)
@@ -439,6 +447,9 @@ def run_batch(args):
     circ_s = len(cs) * args.steps * world / t
 
     # e2e through the C ABI with host buffers: plan + upload (prepare), run, every state read back
+    # in one call into page-locked host arrays
+    ntot = max(1, int(sum(b.nnz(i) for i in range(len(cs)))))
+    out = (pinned(ntot, np.uint64), pinned(ntot, np.float64), pinned(ntot, np.float64))
     e2e_steps = 2
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -447,10 +458,7 @@ def run_batch(args):
         b.prepare(cs)
         b.run()
         b.sync()
-        d2h = 0
-        for i in range(len(cs)):
-            k, r, im = b.state(i, sorted=False)
-            d2h += k.nbytes + r.nbytes + im.nbytes
+        d2h = sum(k.nbytes + r.nbytes + im.nbytes for k, r, im in b.states(out=out))
     e2e_t = (time.perf_counter() - t0) / e2e_steps
     h2d = int(sum(g.nbytes for _, g in cs))
 

@@ -279,6 +279,12 @@ int sqc_batch_nnz(sqc_batch* b, uint32_t i, uint64_t* nnz);
 /* Readout of circuit i, as sqc_get_state. */
 int sqc_batch_get_state(sqc_batch* b, uint32_t i, uint64_t* keys, double* re, double* im, uint64_t cap,
                         uint64_t* n, uint32_t flags);
+/* Readout of every circuit in one call: circuit i's counts[i] entries follow circuit i-1's in
+ * keys/re/im (capacity cap); *total receives the entry count. One readout kernel per circuit
+ * and one copy back per array, so the cost is that of the data, not of n round trips. Flags
+ * as sqc_get_state (SQC_READ_SORTED orders each circuit's entries). */
+int sqc_batch_get_states(sqc_batch* b, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* counts,
+                         uint64_t* total, uint32_t flags);
 /* Time candidate tunings (load factor, chunk size, blocks per SM) on the prepared circuits and
  * keep the fastest. Runs the batch several times; the circuits' states afterwards are those
  * of a complete run. */

@@ -385,6 +385,84 @@ int Batch::ensure_readout(size_t n) {
     return SQC_OK;
 }
 
+int Batch::get_states(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* counts, uint64_t* total,
+                      uint32_t flags) {
+    if (!synced_) return fail(SQC_ERR_STATE, "sync the batch first");
+    const size_t nc = plans_.size();
+    std::vector<unsigned long long> off(nc + 1, 0);
+    for (size_t i = 0; i < nc; ++i) {
+        if (h_ctl_[i].status != ST_OK) return fail(SQC_ERR_STATE, "circuit " + std::to_string(i) + " failed");
+        off[i + 1] = off[i] + h_ctl_[i].nnz;
+    }
+    if (total) *total = off[nc];
+    int rc;
+    if ((rc = ensure_readout(off[nc]))) return rc;
+    // circuit i's readout lands at offset off[i] (its key count bounds what it writes)
+    for (size_t i = 0; i < nc; ++i) {
+        Ctl* ctl = d_ctl_ + i;
+        if ((rc = cuda(cudaMemsetAsync(&ctl->out_count, 0, sizeof(unsigned long long), stream_), "memset"))) return rc;
+        if (!h_ctl_[i].nnz) continue;
+        if ((rc = cuda(launch_readout(tables_[i], ctl, std::max<unsigned long long>(h_ctl_[i].list_n, 1),
+                                      plans_[i].end.frame, dbl_, d_rk_ + off[i], d_rr_ + off[i], d_ri_ + off[i],
+                                      h_ctl_[i].nnz, (flags & SQC_READ_DROP_NEGLIGIBLE) != 0, prune_, sms_, stream_),
+                       "readout")))
+            return rc;
+        ++launches_;
+    }
+    if ((rc = cuda(cudaMemcpyAsync(h_ctl_, d_ctl_, nc * sizeof(Ctl), cudaMemcpyDeviceToHost, stream_), "D2H ctl")) ||
+        (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
+        return rc;
+    uint64_t got = 0;
+    for (size_t i = 0; i < nc; ++i) got += h_ctl_[i].out_count;
+    if (total) *total = got;
+    if (got > cap) return fail(SQC_ERR_CAPACITY, "output arrays too small");
+    if (got && (!keys || !re || !im || !counts)) return fail(SQC_ERR_ARG, "null output array");
+    if (!off[nc]) return SQC_OK;
+    // without dropping, the circuits' entries are already contiguous: one copy per array
+    const bool dense = got == off[nc];
+    if (dense) {
+        if ((rc = cuda(cudaMemcpyAsync(keys, d_rk_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H keys")) ||
+            (rc = cuda(cudaMemcpyAsync(re, d_rr_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H re")) ||
+            (rc = cuda(cudaMemcpyAsync(im, d_ri_, got * 8, cudaMemcpyDeviceToHost, stream_), "D2H im")))
+            return rc;
+    } else {
+        uint64_t at = 0;
+        for (size_t i = 0; i < nc; ++i) {
+            const uint64_t c = h_ctl_[i].out_count;
+            if (c && ((rc = cuda(cudaMemcpyAsync(keys + at, d_rk_ + off[i], c * 8, cudaMemcpyDeviceToHost, stream_),
+                                 "D2H keys")) ||
+                      (rc = cuda(cudaMemcpyAsync(re + at, d_rr_ + off[i], c * 8, cudaMemcpyDeviceToHost, stream_),
+                                 "D2H re")) ||
+                      (rc = cuda(cudaMemcpyAsync(im + at, d_ri_ + off[i], c * 8, cudaMemcpyDeviceToHost, stream_),
+                                 "D2H im"))))
+                return rc;
+            at += c;
+        }
+    }
+    if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
+    uint64_t at = 0;
+    for (size_t i = 0; i < nc; ++i) {
+        const uint64_t c = h_ctl_[i].out_count;
+        counts[i] = c;
+        if ((flags & SQC_READ_SORTED) && c > 1) {   // key order within each circuit
+            std::vector<uint64_t> idx(c);
+            std::iota(idx.begin(), idx.end(), 0);
+            uint64_t* k = keys + at;
+            double* r = re + at;
+            double* im_ = im + at;
+            std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) { return k[a] < k[b]; });
+            std::vector<uint64_t> k2(c);
+            std::vector<double> r2(c), i2(c);
+            for (uint64_t j = 0; j < c; ++j) { k2[j] = k[idx[j]]; r2[j] = r[idx[j]]; i2[j] = im_[idx[j]]; }
+            std::memcpy(k, k2.data(), c * 8);
+            std::memcpy(r, r2.data(), c * 8);
+            std::memcpy(im_, i2.data(), c * 8);
+        }
+        at += c;
+    }
+    return SQC_OK;
+}
+
 int Batch::get_state(uint32_t i, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags) {
     if (i >= plans_.size()) return fail(SQC_ERR_ARG, "bad circuit index");
     if (!synced_) return fail(SQC_ERR_STATE, "sync the batch first");

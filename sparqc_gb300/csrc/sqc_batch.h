@@ -60,6 +60,10 @@ public:
     int circuit_status(uint32_t i, int* status);
     int nnz(uint32_t i, uint64_t* out);
     int get_state(uint32_t i, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
+    // Every circuit's state in one call: circuit i's entries follow circuit i-1's in the
+    // arrays, counts[i] of them; one readout kernel per circuit, one copy back per array.
+    int get_states(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* counts, uint64_t* total,
+                   uint32_t flags);
     int autotune(sqc_batch_tuning* out);
     int stats(sqc_batch_stats* out);
     cudaStream_t stream() const { return stream_; }

@@ -100,6 +100,11 @@ int sqc_batch_get_state(sqc_batch* bt, uint32_t i, uint64_t* keys, double* re, d
     return guarded(bt, [&](sqc::Batch& b) { return b.get_state(i, keys, re, im, cap, n, flags); });
 }
 
+int sqc_batch_get_states(sqc_batch* bt, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* counts,
+                         uint64_t* total, uint32_t flags) {
+    return guarded(bt, [&](sqc::Batch& b) { return b.get_states(keys, re, im, cap, counts, total, flags); });
+}
+
 int sqc_batch_autotune(sqc_batch* bt, sqc_batch_tuning* out) {
     return guarded(bt, [&](sqc::Batch& b) { return b.autotune(out); });
 }

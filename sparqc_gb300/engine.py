@@ -26,6 +26,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_load",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
+           "sqc_batch_get_states",
            "sqc_batch_autotune", "sqc_batch_get_stats", "sqc_batch_compare", "sqc_batch_last_error",
            "sqc_batch_stream",
            "sqc_server_default_options", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
@@ -166,6 +167,7 @@ def load(path=LIB_PATH):
     L.sqc_batch_circuit_status.argtypes = [P, U32, ctypes.POINTER(I)]
     L.sqc_batch_nnz.argtypes = [P, U32, ctypes.POINTER(U64)]
     L.sqc_batch_get_state.argtypes = [P, U32, P, P, P, U64, ctypes.POINTER(U64), U32]
+    L.sqc_batch_get_states.argtypes = [P, P, P, P, U64, P, ctypes.POINTER(U64), U32]
     L.sqc_batch_autotune.argtypes = [P, ctypes.POINTER(BatchTuning)]
     L.sqc_batch_get_stats.argtypes = [P, ctypes.POINTER(BatchStats)]
     L.sqc_batch_last_error.argtypes = [P]
@@ -205,7 +207,8 @@ def load(path=LIB_PATH):
               "sqc_part_sync", "sqc_part_nnz", "sqc_part_get_state", "sqc_part_get_stats"):
         getattr(L, n).restype = I
     for n in ("sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare", "sqc_batch_run", "sqc_batch_sync",
-              "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state", "sqc_batch_autotune",
+              "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state", "sqc_batch_get_states",
+              "sqc_batch_autotune",
               "sqc_batch_get_stats", "sqc_server_create", "sqc_server_destroy", "sqc_server_submit",
               "sqc_server_step", "sqc_server_completed", "sqc_server_request_status", "sqc_server_nnz",
               "sqc_server_get_state", "sqc_server_release", "sqc_server_get_stats", "sqc_batch_compare",
@@ -502,6 +505,26 @@ class Batch:
                     "batch get_state")
         m = got.value
         return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def states(self, sorted=False, drop_negligible=False, out=None):
+        """Every circuit's state in one call: a list of (keys, re, im) views into three arrays.
+        out: optional (keys, re, im) arrays to fill (e.g. page-locked), large enough for every
+        circuit's keys."""
+        n = int(sum(self.nnz(i) for i in range(self.n)))
+        if out is None:
+            out = (np.empty(max(n, 1), np.uint64), np.empty(max(n, 1), np.float64), np.empty(max(n, 1), np.float64))
+        keys, re, im = out
+        counts = np.zeros(max(self.n, 1), np.uint64)
+        total = ctypes.c_uint64()
+        flags = (READ_SORTED if sorted else 0) | (READ_DROP_NEGLIGIBLE if drop_negligible else 0)
+        self._check(self._L.sqc_batch_get_states(self._h, _p(keys), _p(re), _p(im), keys.size, _p(counts),
+                                                 ctypes.byref(total), flags), "batch get_states")
+        res, at = [], 0
+        for i in range(self.n):
+            c = int(counts[i])
+            res.append((keys[at:at + c], re[at:at + c], im[at:at + c]))
+            at += c
+        return res
 
     def compare(self, i, ref):
         """(fidelity, max abs error) of circuit i against a State of the same qubit count."""

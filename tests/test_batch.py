@@ -43,6 +43,26 @@ def test_batch_matches_each_circuit_alone(precision):
     b.close()
 
 
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_batch_readout_of_every_circuit_in_one_call(precision):
+    cs = _mixed(30, 5)
+    b = Batch(precision=precision)
+    b.prepare(cs)
+    b.run()
+    b.sync()
+    sorted_all = b.states(sorted=True)
+    assert len(sorted_all) == len(cs)
+    for i in range(len(cs)):
+        assert _same(sorted_all[i], b.state(i)), f"circuit {i}"
+    # unsorted: the same entries per circuit; dropping negligible entries as get_state does
+    for i, (k, r, im) in enumerate(b.states()):
+        order = np.argsort(k)
+        assert _same((k[order], r[order], im[order]), b.state(i)), f"circuit {i}"
+    for i, got in enumerate(b.states(sorted=True, drop_negligible=True)):
+        assert _same(got, b.state(i, drop_negligible=True)), f"circuit {i}"
+    b.close()
+
+
 def test_batch_matches_oracle():
     from oracle.sparse import SparseOracle
     cs = _mixed(6, 2, qrange=(10, 30), krange=(4, 10), drange=(50, 150))
