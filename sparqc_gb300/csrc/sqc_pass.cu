@@ -98,6 +98,9 @@ template <class T, int NX> struct StagedOcc {
     static constexpr int kMin = sizeof(T) == 8 ? (NX == 3 ? 4 : 6) : 0;   // FP64 octets: 53 KB rings, four blocks
 };
 template <class T> struct StageGates { static constexpr bool kOn = sizeof(T) == 8; };
+// The direct kernel's FP32 octet passes also gain from it (1.7% on the 40-qubit workload); the
+// staged kernel's lose (3.5%).
+template <class T, int NX> struct DirectStage { static constexpr bool kOn = sizeof(T) == 8 || NX == 3; };
 
 // Octet passes (three cross-group qubits) hold four slots per lane: FP64 two blocks, FP32 three.
 template <class T, int NX> struct DirectOcc {
@@ -113,8 +116,8 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
         return;
     }
-    __shared__ SmemGate sg[StageGates<T>::kOn ? kMaxRun : 1];
-    if constexpr (StageGates<T>::kOn) stage_gates(sg, a.gates, a.g0, a.g1);
+    __shared__ SmemGate sg[DirectStage<T, NX>::kOn ? kMaxRun : 1];
+    if constexpr (DirectStage<T, NX>::kOn) stage_gates(sg, a.gates, a.g0, a.g1);
     const unsigned ep = ctl->epoch;
     const unsigned long long nnz_in = ctl->nnz;
     const TableDev t = a.t;
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
             long long mb;
             unsigned long long G0;
             const unsigned om = units4<3>(t, ep, e0, n, m1, m2, lane, &mb, &G0, m3);
-            run_units8<T, StageGates<T>::kOn>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, m3, om, mb, G0, lane,
+            run_units8<T, DirectStage<T, NX>::kOn>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, m3, om, mb, G0, lane,
                                               a.prune, cnt_nnz, cnt_empty, upd);
         }
     } else {
@@ -170,11 +173,18 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
 constexpr int kResolveThreads = 256;
 
 // ---- resolve: the owned units of a pass that pairs groups, before the pass -----------------
-// Every thread settles ownership for one list entry (all lookups of a block in flight at
-// once); each block reserves room for its owned units with one atomic on ctl->units_n and
-// writes them densely, in no particular order. The staged pass deals the units out evenly.
+// Two phases per chunk of kResolveThreads list entries:
+//  * ownership: every thread takes one entry and looks up the unit's members of smaller index
+//    (the entry owns its unit iff none is live; usually one lookup settles it). Each block
+//    reserves room for its owned units with one atomic on ctl->units_n and places them
+//    densely, in no particular order;
+//  * members: the owners' remaining lookups are spread over the warp's lanes, K = 2^nx lanes
+//    per owner (lane k looks up member k), 32 / K owners at a time, so an owner's members are
+//    found in one round trip rather than one after another.
+// The staged pass deals the units out evenly.
 template <int NX>
 __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
+    constexpr int K = 1 << NX;
     __shared__ unsigned warp_at[kResolveThreads / 32];
     __shared__ unsigned long long base_sh;
     Ctl* ctl = a.ctl;
@@ -188,19 +198,25 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
     const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
     const unsigned long long m2 = NX >= 2 ? 1ULL << (a.q2 - kSlotBits) : 0ULL;
     const unsigned long long m3 = NX == 3 ? 1ULL << (a.q3 - kSlotBits) : 0ULL;
+    auto member = [&](unsigned long long G0, int k) {
+        return G0 | ((k & 1) ? m1 : 0ULL) | ((k & 2) ? m2 : 0ULL) | ((k & 4) ? m3 : 0ULL);
+    };
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (unsigned long long c0 = (unsigned long long)blockIdx.x * kResolveThreads; c0 < n;
          c0 += (unsigned long long)gridDim.x * kResolveThreads) {
         const unsigned long long e = c0 + threadIdx.x;
-        Unit u;
         bool own = false;
+        unsigned b = kNoBucket;
+        int idx = 0;
+        unsigned long long G0 = 0;
         if (e < n) {
-            const unsigned b = t.list[e];
-            long long bk[8];
-            own = unit_owner<NX>(t, ep, load_hdr(t.hdr + b).group, (long long)b, m1, m2, m3, bk, &u.G0);
-#pragma unroll
-            for (int k = 0; k < 8; ++k) u.b[k] = bk[k] < 0 ? kNoBucket : (unsigned)bk[k];
+            b = t.list[e];
+            const unsigned long long G = load_hdr(t.hdr + b).group;
+            idx = ((G & m1) ? 1 : 0) | ((NX >= 2 && (G & m2)) ? 2 : 0) | ((NX == 3 && (G & m3)) ? 4 : 0);
+            G0 = G & ~(m1 | m2 | m3);
+            own = true;
+            for (int k = 0; k < idx && own; ++k) own = lookup_group(t, ep, member(G0, k)) < 0;
         }
         const unsigned bal = __ballot_sync(kFull, own);
         if (lane == 0) warp_at[w] = __popc(bal);
@@ -215,7 +231,30 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
             base_sh = tot ? atomicAdd(&ctl->units_n, (unsigned long long)tot) : 0ULL;
         }
         __syncthreads();
-        if (own) t.units[base_sh + warp_at[w] + __popc(bal & ((1u << lane) - 1u))] = u;
+        const unsigned long long pos = base_sh + warp_at[w] + __popc(bal & ((1u << lane) - 1u));
+        // members of this warp's owners, 32 / K owners per round, lane r * K + k on member k
+        unsigned rem = bal;
+        while (rem) {
+            int src = -1;
+#pragma unroll
+            for (int r = 0; r < 32 / K; ++r) {
+                const int o = rem ? __ffs(rem) - 1 : -1;
+                if (rem) rem &= rem - 1;
+                if (r == lane / K) src = o;
+            }
+            const int k = lane % K;
+            const unsigned long long sG0 = shfl64(G0, src < 0 ? 0 : src);
+            const int sidx = __shfl_sync(kFull, idx, src < 0 ? 0 : src);
+            const unsigned sb = __shfl_sync(kFull, b, src < 0 ? 0 : src);
+            const unsigned long long spos = shfl64(pos, src < 0 ? 0 : src);
+            if (src >= 0) {
+                // members below the owner's index are absent (that is what made it the owner)
+                const long long mb = k == sidx ? (long long)sb : k < sidx ? -1LL : lookup_group(t, ep, member(sG0, k));
+                Unit* u = t.units + spos;
+                u->b[k] = mb < 0 ? kNoBucket : (unsigned)mb;
+                if (k == 0) u->G0 = sG0;
+            }
+        }
         __syncthreads();   // warp_at and base_sh are reused by the next chunk
     }
 }
