@@ -16,6 +16,7 @@ namespace {
 
 constexpr unsigned long long kMinBuckets = 64;
 constexpr size_t kFlushAt = 1024;          // queued gates that trigger a launch
+constexpr unsigned long long kTinyMaxList = 256;   // live buckets up to which a flush is one launch
 constexpr size_t kDescInitial = 1 << 14;   // descriptors held between verified syncs
 constexpr double kMaxLoad = 0.9;           // live buckets a pair pass may leave behind
 
@@ -35,6 +36,8 @@ Engine::~Engine() {
     if (ctl_host_) cudaFreeHost(ctl_host_);
     if (d_desc_) cudaFree(d_desc_);
     if (h_desc_) cudaFreeHost(h_desc_);
+    if (d_tiny_) cudaFree(d_tiny_);
+    if (h_tiny_) cudaFreeHost(h_tiny_);
     if (d_rk_) cudaFree(d_rk_);
     if (d_rr_) cudaFree(d_rr_);
     if (d_ri_) cudaFree(d_ri_);
@@ -167,12 +170,19 @@ int Engine::ensure_desc(size_t n) {
     const size_t cap = std::max(n, desc_cap_ * 2);
     if (d_desc_) cudaFree(d_desc_);
     if (h_desc_) cudaFreeHost(h_desc_);
+    if (d_tiny_) cudaFree(d_tiny_);
+    if (h_tiny_) cudaFreeHost(h_tiny_);
     d_desc_ = nullptr;
     h_desc_ = nullptr;
+    d_tiny_ = nullptr;
+    h_tiny_ = nullptr;
     desc_cap_ = 0;
     int rc;
     if ((rc = cuda(cudaMalloc(&d_desc_, cap * sizeof(GateDesc)), "cudaMalloc(desc)"))) return rc;
     if ((rc = cuda(cudaMallocHost(&h_desc_, cap * sizeof(GateDesc)), "cudaMallocHost(desc)"))) return rc;
+    // tiny-launch pass records, indexed like the descriptors (a flush has no more passes than gates)
+    if ((rc = cuda(cudaMalloc(&d_tiny_, cap * sizeof(TinyPass)), "cudaMalloc(tiny)"))) return rc;
+    if ((rc = cuda(cudaMallocHost(&h_tiny_, cap * sizeof(TinyPass)), "cudaMallocHost(tiny)"))) return rc;
     desc_cap_ = cap;
     return SQC_OK;
 }
@@ -350,6 +360,54 @@ int Engine::flush() {
         return rc;
     cudaEvent_t ev_prev = nullptr;
     if (time_passes_ && (rc = record_event(&ev_prev))) return rc;
+    // a tiny state runs the flush's passes in one single-block launch (tiny_kernel): the live
+    // buckets every pass may reach stay few enough that launches would cost more than the work
+    {
+        unsigned long long h = list_hint_, hmax = list_hint_;
+        for (const Span& sp : spans) {
+            if (sp.nx) h = std::min<unsigned long long>(tab_.nb, std::min(h << sp.nx, group_bound(after[sp.g1 - 1], nq_)));
+            hmax = std::max(hmax, h);
+        }
+        if (spans.size() >= 2 && tiny_table(tab_.nb) && hmax <= kTinyMaxList) {
+            TinyPass* ht = h_tiny_ + desc_used_;
+            bool any_pair = false;
+            for (size_t k = 0; k < spans.size(); ++k) {
+                const Span& sp = spans[k];
+                TinyPass& q = ht[k];
+                q.g0 = (uint32_t)sp.g0;
+                q.g1 = (uint32_t)sp.g1;
+                q.nx = sp.nx;
+                q.q1 = sp.q1;
+                q.q2 = sp.q2;
+                q.q3 = sp.q3;
+                q.keys_fixed = sp.fixed ? 1u : 0u;
+                q.pad = 0;
+                q.grow_bound = group_bound(after[sp.g1 - 1], nq_);
+                any_pair = any_pair || sp.nx > 0;
+            }
+            if ((rc = cuda(cudaMemcpyAsync(d_tiny_ + desc_used_, ht, spans.size() * sizeof(TinyPass),
+                                           cudaMemcpyHostToDevice, stream_), "H2D tiny passes")))
+                return rc;
+            if (launch_tiny(a, d_tiny_ + desc_used_, (uint32_t)spans.size(), dbl_, stream_) < 0)
+                return cuda(cudaGetLastError(), "tiny passes");
+            if (time_passes_) {
+                cudaEvent_t ev = nullptr;
+                if ((rc = record_event(&ev))) return rc;
+                timed_.push_back(TimedPass{ev_prev, ev, any_pair});
+            }
+            for (const Span& sp : spans) {
+                passes_pair_ += sp.nx > 0 ? 1 : 0;
+                passes_.push_back(PassRec{snap_log_, snap_plan_});
+                snap_log_ = src[sp.g1 - 1] + 1;
+                snap_plan_ = after[sp.g1 - 1];
+                ++passes_run_;
+            }
+            ++launches_;
+            list_hint_ = h;
+            desc_used_ += nd;
+            return SQC_OK;
+        }
+    }
     for (const Span& sp : spans) {
         const size_t i = sp.g1;
         a.g0 = (uint32_t)sp.g0;

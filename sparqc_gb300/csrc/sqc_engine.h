@@ -130,6 +130,8 @@ private:
 
     GateDesc* d_desc_ = nullptr;
     GateDesc* h_desc_ = nullptr;
+    TinyPass* d_tiny_ = nullptr;    // pass records of single-launch flushes (tiny states)
+    TinyPass* h_tiny_ = nullptr;
     size_t desc_cap_ = 0, desc_used_ = 0;
 
     unsigned long long* d_rk_ = nullptr;

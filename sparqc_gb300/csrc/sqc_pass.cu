@@ -107,31 +107,18 @@ template <class T, int NX> struct DirectOcc {
     static constexpr int kMin = NX == 3 ? (sizeof(T) == 8 ? 2 : 3) : (sizeof(T) == 8 ? 3 : 4);
 };
 
-template <class T, int NX>
-__global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kernel(PassArgs a) {
+// The work of one direct pass: warps take four list entries at a time through next4 (a value
+// >= n ends the pass), so they finish together whatever the number of units each group of
+// entries owns. sg holds the pass's gates when DirectStage is on. Counters accumulate per thread.
+template <class T, int NX, bool SMEM, class Next>
+__device__ __forceinline__ void direct_work(const PassArgs& a, const SmemGate* sg, unsigned ep, unsigned long long n,
+                                            Next&& next4, unsigned long long& cnt_nnz, unsigned long long& cnt_empty,
+                                            unsigned long long& upd) {
     Ctl* ctl = a.ctl;
-    if (*(volatile unsigned int*)&ctl->status) return;
-    const unsigned long long n = ctl->list_n;
-    if (NX > 0 && could_overflow(a, n)) {   // refuse before touching the state
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
-        return;
-    }
-    __shared__ SmemGate sg[DirectStage<T, NX>::kOn ? kMaxRun : 1];
-    if constexpr (DirectStage<T, NX>::kOn) stage_gates(sg, a.gates, a.g0, a.g1);
-    const unsigned ep = ctl->epoch;
-    const unsigned long long nnz_in = ctl->nnz;
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, half = lane >> 4, j = lane & 15;
-    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
     Val<T> va, vb;
-    // warps take four list entries at a time from the pass's work counter, so they finish
-    // together whatever the number of units each group of entries owns
-    auto next4 = [&]() -> unsigned long long {
-        unsigned long long e = 0;
-        if (lane == 0) e = atomicAdd(&ctl->work, 4ULL);
-        return shfl64(e, 0);
-    };
-    if (NX == 0) {
+    if constexpr (NX == 0) {
         for (unsigned long long e0 = next4(); e0 < n; e0 = next4()) {
             const unsigned long long ea = e0 + 2 * half, eb = ea + 1;
             const long long ba = ea < n ? (long long)t.list[ea] : -1;
@@ -140,7 +127,7 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
             const unsigned long long Gb = bb >= 0 ? load_hdr(t.hdr + bb).group : 0ULL;
             load_val_g<T>(t, va, Ga, ba, j);
             load_val_g<T>(t, vb, Gb, bb, j);
-            if constexpr (StageGates<T>::kOn) run_gates_s<T>(sg, a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
+            if constexpr (SMEM) run_gates_s<T>(sg, a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
             else run_gates<T>(a.gates, a.g0, a.g1, va, vb, lane, a.prune, upd);
             write_val<T>(t, ep, va, lane, &ctl->status, cnt_nnz, cnt_empty);
             write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
@@ -153,8 +140,8 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
             long long mb;
             unsigned long long G0;
             const unsigned om = units4<3>(t, ep, e0, n, m1, m2, lane, &mb, &G0, m3);
-            run_units8<T, DirectStage<T, NX>::kOn>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, m3, om, mb, G0, lane,
-                                              a.prune, cnt_nnz, cnt_empty, upd);
+            run_units8<T, SMEM>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, m3, om, mb, G0, lane, a.prune, cnt_nnz,
+                                cnt_empty, upd);
         }
     } else {
         const unsigned long long m1 = 1ULL << (a.q1 - kSlotBits);
@@ -163,11 +150,109 @@ __global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kerne
             long long mb;
             unsigned long long G0;
             const unsigned om = units4<NX>(t, ep, e0, n, m1, m2, lane, &mb, &G0);
-            run_units4<T, NX, true, StageGates<T>::kOn>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, om, mb, G0, lane,
-                                                        a.prune, va, vb, cnt_nnz, cnt_empty, upd);
+            run_units4<T, NX, true, SMEM>(t, ep, ctl, a.gates, sg, a.g0, a.g1, m1, m2, om, mb, G0, lane, a.prune, va,
+                                          vb, cnt_nnz, cnt_empty, upd);
         }
     }
+}
+
+template <class T, int NX>
+__global__ void __launch_bounds__(kThreads, DirectOcc<T, NX>::kMin) direct_kernel(PassArgs a) {
+    Ctl* ctl = a.ctl;
+    if (*(volatile unsigned int*)&ctl->status) return;
+    const unsigned long long n = ctl->list_n;
+    if (NX > 0 && could_overflow(a, n)) {   // refuse before touching the state
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
+        return;
+    }
+    constexpr bool kSmem = NX == 3 ? DirectStage<T, NX>::kOn : StageGates<T>::kOn;
+    __shared__ SmemGate sg[kSmem ? kMaxRun : 1];
+    if constexpr (kSmem) stage_gates(sg, a.gates, a.g0, a.g1);
+    const unsigned ep = ctl->epoch;
+    const unsigned long long nnz_in = ctl->nnz;
+    const int lane = threadIdx.x & 31;
+    unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
+    auto next4 = [&]() -> unsigned long long {
+        unsigned long long e = 0;
+        if (lane == 0) e = atomicAdd(&ctl->work, 4ULL);
+        return shfl64(e, 0);
+    };
+    direct_work<T, NX, kSmem>(a, sg, ep, n, next4, cnt_nnz, cnt_empty, upd);
     finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
+}
+
+// ---- tiny states: every pass of a flush in one single-block launch --------------------------
+// For tables of at most kTinyMaxBuckets buckets a pass is a few microseconds of dependent
+// loads, and separate launches would cost more than the work. One block runs the passes in
+// order: the pass's gates are staged in shared memory, warps claim list entries from a
+// shared-memory counter, the block reduces and publishes the pass (as finish_pass does) and
+// synchronises before the next. A pass that could overflow the table refuses as a direct pass
+// does, and the passes after it do not run; the host repairs and replays from there.
+template <class T>
+__global__ void __launch_bounds__(kThreads) tiny_kernel(PassArgs a, const TinyPass* __restrict__ tp, uint32_t np) {
+    __shared__ SmemGate sg[kMaxRun];
+    __shared__ unsigned long long claim_sh;
+    __shared__ unsigned long long red[3][kThreads / 32];
+    __shared__ int stop;
+    Ctl* ctl = a.ctl;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t p = 0; p < np; ++p) {
+        if (threadIdx.x == 0) {
+            stop = *(volatile unsigned int*)&ctl->status != 0;
+            claim_sh = 0;
+        }
+        __syncthreads();
+        if (stop) return;
+        PassArgs b = a;
+        const TinyPass q = tp[p];
+        b.g0 = q.g0;
+        b.g1 = q.g1;
+        b.nx = q.nx;
+        b.q1 = q.q1;
+        b.q2 = q.q2;
+        b.q3 = q.q3;
+        b.keys_fixed = q.keys_fixed;
+        b.grow_bound = q.grow_bound;
+        const unsigned long long n = *(volatile unsigned long long*)&ctl->list_n;
+        if (b.nx > 0 && could_overflow(b, n)) {   // refuse before touching the state
+            if (threadIdx.x == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_GROW);
+            return;
+        }
+        stage_gates(sg, b.gates, b.g0, b.g1);
+        const unsigned ep = *(volatile unsigned int*)&ctl->epoch;
+        const unsigned long long nnz_in = *(volatile unsigned long long*)&ctl->nnz;
+        unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
+        auto next4 = [&]() -> unsigned long long {
+            unsigned long long e = 0;
+            if (lane == 0) e = atomicAdd(&claim_sh, 4ULL);
+            return shfl64(e, 0);
+        };
+        switch (b.nx) {
+        case 0: direct_work<T, 0, true>(b, sg, ep, n, next4, cnt_nnz, cnt_empty, upd); break;
+        case 1: direct_work<T, 1, true>(b, sg, ep, n, next4, cnt_nnz, cnt_empty, upd); break;
+        case 2: direct_work<T, 2, true>(b, sg, ep, n, next4, cnt_nnz, cnt_empty, upd); break;
+        default: direct_work<T, 3, true>(b, sg, ep, n, next4, cnt_nnz, cnt_empty, upd); break;
+        }
+        cnt_nnz = warp_sum(cnt_nnz);
+        cnt_empty = warp_sum(cnt_empty);
+        upd = warp_sum(upd);
+        if (lane == 0) { red[0][w] = cnt_nnz; red[1][w] = cnt_empty; red[2][w] = upd; }
+        __syncthreads();
+        if (threadIdx.x == 0 && *(volatile unsigned int*)&ctl->status == 0) {
+            unsigned long long tn = 0, te = 0, tu = 0;
+            for (int i = 0; i < kThreads / 32; ++i) { tn += red[0][i]; te += red[1][i]; tu += red[2][i]; }
+            ctl->nnz = tn;
+            ctl->empty_groups = te;
+            ctl->list_n = *(volatile unsigned long long*)&ctl->list_tail;
+            ctl->amp_updates += tu;
+            const unsigned long long ab = b.keys_fixed ? nnz_in * (8ULL + 2ULL * b.amp_bytes)
+                                                       : (nnz_in + tn) * (8ULL + b.amp_bytes);
+            ctl->alg_bytes += ab;
+            if (b.nx > 0) ctl->alg_bytes_pair += ab;
+            ctl->seq += 1;
+        }
+        __syncthreads();   // the pass is published before the next one reads it
+    }
 }
 
 constexpr int kResolveThreads = 256;
@@ -521,6 +606,8 @@ int direct_residency(bool dbl, int nx) {
     return c;
 }
 
+constexpr unsigned long long kTinyMaxBuckets = 4096;
+
 template <class T, int NX>
 void launch_direct(const PassArgs& a, int grid, cudaStream_t st) {
     direct_kernel<T, NX><<<grid, kThreads, 0, st>>>(a);
@@ -532,6 +619,15 @@ void launch_staged(const PassArgs& a, int grid, cudaStream_t st) {
 }
 
 }  // namespace
+
+bool tiny_table(unsigned long long buckets) { return buckets <= kTinyMaxBuckets; }
+
+int launch_tiny(const PassArgs& a, const TinyPass* passes, uint32_t np, bool dbl, cudaStream_t st) {
+    if (a.t.mask + 1 > kTinyMaxBuckets) return -1;
+    if (dbl) tiny_kernel<double><<<1, kThreads, 0, st>>>(a, passes, np);
+    else tiny_kernel<float><<<1, kThreads, 0, st>>>(a, passes, np);
+    return cudaGetLastError() == cudaSuccess ? 1 : -1;
+}
 
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
     // list_hint bounds the live-bucket count; grids are sized from it (one resident wave at

@@ -107,6 +107,12 @@ struct PruneBits {
 
 constexpr uint32_t kNoQubit = 0xFFFFFFFFu;
 
+// One pass of a single-launch run over a tiny table (tiny_kernel): what PassArgs says per pass.
+struct TinyPass {
+    uint32_t g0, g1, nx, q1, q2, q3, keys_fixed, pad;
+    unsigned long long grow_bound;
+};
+
 struct PassArgs {
     TableDev t;
     Ctl* ctl;
