@@ -174,7 +174,7 @@ def read_profile(name):
 
 
 def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured, precision, profile_name):
-    """Roofline of the dominant gate-pass kernel over the timed steps.
+    """Roofline of the dominant gate-pass kernel over steps whose passes are timed one by one.
 
     Every pass is bracketed by CUDA events on the engine's stream (time_passes); pair passes
     (one direct_kernel<T, true> launch, or resolve_kernel + staged_kernel<T, true> on large
@@ -288,22 +288,39 @@ def run_gpu(args):
     # one stream for everything timed: the L2 flush, the events and the engine's kernels
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    st = engine.State(nq, precision=args.precision, stream=stream.cuda_stream,
-                      initial_buckets=1 << max(6, p["k"] - 4 + 1), time_passes=True)
-    if st.stream != stream.cuda_stream:
-        raise RuntimeError("the engine does not run on the timed stream")
-    # warm-up: grows the tables to their final size and fixes the per-step counters
-    for _ in range(max(3, args.warmup)):
-        sw = st.stats()
-        st.set_zero()
-        st.apply(gates)
-        st.sync()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def make_state(time_passes):
+        s = engine.State(nq, precision=args.precision, stream=stream.cuda_stream,
+                         initial_buckets=1 << max(6, p["k"] - 4 + 1), time_passes=time_passes)
+        if s.stream != stream.cuda_stream:
+            raise RuntimeError("the engine does not run on the timed stream")
+        # warm-up: grows the tables to their final size and fixes the per-step counters
+        for _ in range(max(3, args.warmup)):
+            sw = s.stats()
+            s.set_zero()
+            s.apply(gates)
+            s.sync()
+        return s, sw
+
+    def timed_steps(s, ev):
+        # one step: flush L2, then the circuit from |0..0>, bracketed by events on the stream
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            s.set_zero()
+            s.apply(gates)
+            s.flush()
+            ev[i][1].record(stream)
+
+    # the measured steps run with no per-pass events: consecutive passes then overlap the next
+    # pass's launch with the running pass's tail (programmatic dependent launch)
+    st, sw = make_state(False)
     s0 = st.stats()
     upd_per_step = s0["amp_updates"]
     alg_per_step = s0["alg_bytes"]
     alg_pair_step = s0["alg_bytes_pair"]
     passes_per_step = s0["passes"] - sw["passes"]
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = st.stats()["kernel_launches"]
     if world > 1:
@@ -311,13 +328,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local) if rank == 0 else None
     t_wall0 = time.perf_counter()
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        ev[i][0].record(stream)
-        st.set_zero()
-        st.apply(gates)
-        st.flush()
-        ev[i][1].record(stream)
+    timed_steps(st, ev)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop() if clocks else None
@@ -364,12 +375,27 @@ def run_gpu(args):
            "h2d_bytes_per_step": int(gates.size * 136), "d2h_bytes_per_step": int(nout * 24),
            "path": "sqc_set_zero_state + sqc_apply_gates (host gate array) + sqc_get_state (host arrays)"}
 
+    # the kernel durations of the roofline: the same steps again, every pass bracketed by CUDA
+    # events (time_passes), on a second state of the same circuit
+    stt, _ = make_state(True)
+    r0 = stt.stats()
+    evt = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    timed_steps(stt, evt)
+    stt.sync()
+    r1 = stt.stats()
+    dev_ms_t = sum(a.elapsed_time(b) for a, b in evt)
+    stt.close()
+
     if rank != 0:
         return
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    roofline = pass_roofline(s0, s1, alg_per_step, alg_pair_step, args.steps, dev_ms, peak, peaks is not None,
+    roofline = pass_roofline(r0, r1, alg_per_step, alg_pair_step, args.steps, dev_ms_t, peak, peaks is not None,
                              args.precision, profile_for(args, s1["buckets"] > (1 << 20)))
+    roofline["pass_timing"] = ("per-pass CUDA events over the same number of further steps of the same circuit "
+                               "(events between passes stop the launch overlap of the measured steps)")
+    roofline["ms_per_step_with_pass_events"] = dev_ms_t / args.steps
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(gates, args.cpu_seconds, args.precision)
