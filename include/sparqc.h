@@ -91,7 +91,9 @@ typedef struct sqc_options {
     uint32_t device;           /* CUDA device ordinal, default 0 */
     uint32_t max_fused_gates;  /* cap on gates fused into one pass, 0 = default (64) */
     uint32_t time_passes;      /* 1: bracket every gate pass with CUDA events on the handle's stream
-                                  (sqc_stats.pass_ns_*); 0 (default): no events */
+                                  (sqc_stats.pass_ns_*); the events keep consecutive passes from
+                                  overlapping one's launch with the other's drain, and cost ~4-9%
+                                  of a many-pass circuit. 0 (default): no events */
     uint32_t max_cross_qubits; /* qubits >= 4 one pass may pair keys across (branching or swap gates on
                                   them), 1, 2 or 3; 0 = default (3 for FP32, 2 for FP64). Results do
                                   not depend on it. */
