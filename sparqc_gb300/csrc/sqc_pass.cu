@@ -109,7 +109,8 @@ template <class T, int NX> struct DirectOcc {
 
 // The work of one direct pass: warps take four list entries at a time through next4 (a value
 // >= n ends the pass), so they finish together whatever the number of units each group of
-// entries owns. sg holds the pass's gates when DirectStage is on. Counters accumulate per thread.
+// entries owns. With SMEM the gates are read from shared memory (sg[i] = gate g0 + i), else
+// through L1. Counters accumulate per thread.
 template <class T, int NX, bool SMEM, class Next>
 __device__ __forceinline__ void direct_work(const PassArgs& a, const SmemGate* sg, unsigned ep, unsigned long long n,
                                             Next&& next4, unsigned long long& cnt_nnz, unsigned long long& cnt_empty,
