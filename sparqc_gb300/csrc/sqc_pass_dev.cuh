@@ -226,14 +226,14 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
         case KY: gate_on<T, KY>(g, h, a, b, pb); break;
         case KZ: gate_on<T, KZ>(g, h, a, b, pb); break;
         case KH: gate_on<T, KH>(g, h, a, b, pb); break;
-        case KPHASE: gate_on<T, KPHASE>(g, h, a, b, pb); break;
+        case KPHASE:
+        case KT:
+        case KTDG: gate_on<T, KPHASE>(g, h, a, b, pb); break;   // T, Tdg: Phase with their (c, s)
         case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
         case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
         case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
         case KS: gate_on<T, KS>(g, h, a, b, pb); break;
         case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
-        case KT: gate_on<T, KT>(g, h, a, b, pb); break;
-        case KTDG: gate_on<T, KTDG>(g, h, a, b, pb); break;
         case KU: gate_on<T, KU>(g, h, a, b, pb); break;
         default: gate_on<T, KYPH>(g, h, a, b, pb); break;
         }
@@ -320,14 +320,14 @@ __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* 
         case KY: gate_on<T, KY>(g, h, a, b, pb); break;
         case KZ: gate_on<T, KZ>(g, h, a, b, pb); break;
         case KH: gate_on<T, KH>(g, h, a, b, pb); break;
-        case KPHASE: gate_on<T, KPHASE>(g, h, a, b, pb); break;
+        case KPHASE:
+        case KT:
+        case KTDG: gate_on<T, KPHASE>(g, h, a, b, pb); break;   // T, Tdg: Phase with their (c, s)
         case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
         case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
         case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
         case KS: gate_on<T, KS>(g, h, a, b, pb); break;
         case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
-        case KT: gate_on<T, KT>(g, h, a, b, pb); break;
-        case KTDG: gate_on<T, KTDG>(g, h, a, b, pb); break;
         case KU: gate_on<T, KU>(g, h, a, b, pb); break;
         default: gate_on<T, KYPH>(g, h, a, b, pb); break;
         }
@@ -580,14 +580,14 @@ __device__ __forceinline__ void run_gates4(const SmemGate* sg, const GateDesc* _
             case KY: gate_on4<T, KY>(g, h, a, b, c, d, pb); break;
             case KZ: gate_on4<T, KZ>(g, h, a, b, c, d, pb); break;
             case KH: gate_on4<T, KH>(g, h, a, b, c, d, pb); break;
-            case KPHASE: gate_on4<T, KPHASE>(g, h, a, b, c, d, pb); break;
+            case KPHASE:
+            case KT:
+            case KTDG: gate_on4<T, KPHASE>(g, h, a, b, c, d, pb); break;   // T, Tdg: Phase with their (c, s)
             case KRZ: gate_on4<T, KRZ>(g, h, a, b, c, d, pb); break;
             case KRX: gate_on4<T, KRX>(g, h, a, b, c, d, pb); break;
             case KRY: gate_on4<T, KRY>(g, h, a, b, c, d, pb); break;
             case KS: gate_on4<T, KS>(g, h, a, b, c, d, pb); break;
             case KSDG: gate_on4<T, KSDG>(g, h, a, b, c, d, pb); break;
-            case KT: gate_on4<T, KT>(g, h, a, b, c, d, pb); break;
-            case KTDG: gate_on4<T, KTDG>(g, h, a, b, c, d, pb); break;
             case KU: gate_on4<T, KU>(g, h, a, b, c, d, pb); break;
             default: gate_on4<T, KYPH>(g, h, a, b, c, d, pb); break;
             }
