@@ -118,8 +118,11 @@ __device__ __forceinline__ void diag_step(const G& g, const GateHead& h, Val<T>&
     const bool one_sided = K == KANY ? (h.op & kOpOneSided) != 0 : one_sided_kind(K);
     const bool need = v.pres && (!one_sided || bit) && slot_sat(h, v.key);
     if (warp_needs<T>(need)) {
-        const Cx<T> o = K == KANY ? diag_update_rt<T>(h.kind, g, bit, v.amp)
-                                  : diag_update<T, K == KANY ? KZ : K>(g, bit, v.amp);
+        Cx<T> o = K == KANY ? diag_update_rt<T>(h.kind, g, bit, v.amp)
+                            : diag_update<T, K == KANY ? KZ : K>(g, bit, v.amp);
+        if constexpr (K == KS) {   // Sdg runs S's code: its result is S's negated (exact)
+            if (h.kind == KSDG) o = Cx<T>{neg(o.r), neg(o.i)};
+        }
         if (need) { v.amp = o; v.dirty = true; }
     }
 }
@@ -232,8 +235,8 @@ __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, ui
         case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
         case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
         case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
-        case KS: gate_on<T, KS>(g, h, a, b, pb); break;
-        case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
+        case KS:
+        case KSDG: gate_on<T, KS>(g, h, a, b, pb); break;   // Sdg: S negated
         case KU: gate_on<T, KU>(g, h, a, b, pb); break;
         default: gate_on<T, KYPH>(g, h, a, b, pb); break;
         }
@@ -326,8 +329,8 @@ __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* 
         case KRZ: gate_on<T, KRZ>(g, h, a, b, pb); break;
         case KRX: gate_on<T, KRX>(g, h, a, b, pb); break;
         case KRY: gate_on<T, KRY>(g, h, a, b, pb); break;
-        case KS: gate_on<T, KS>(g, h, a, b, pb); break;
-        case KSDG: gate_on<T, KSDG>(g, h, a, b, pb); break;
+        case KS:
+        case KSDG: gate_on<T, KS>(g, h, a, b, pb); break;   // Sdg: S negated
         case KU: gate_on<T, KU>(g, h, a, b, pb); break;
         default: gate_on<T, KYPH>(g, h, a, b, pb); break;
         }
@@ -586,8 +589,8 @@ __device__ __forceinline__ void run_gates4(const SmemGate* sg, const GateDesc* _
             case KRZ: gate_on4<T, KRZ>(g, h, a, b, c, d, pb); break;
             case KRX: gate_on4<T, KRX>(g, h, a, b, c, d, pb); break;
             case KRY: gate_on4<T, KRY>(g, h, a, b, c, d, pb); break;
-            case KS: gate_on4<T, KS>(g, h, a, b, c, d, pb); break;
-            case KSDG: gate_on4<T, KSDG>(g, h, a, b, c, d, pb); break;
+            case KS:
+            case KSDG: gate_on4<T, KS>(g, h, a, b, c, d, pb); break;   // Sdg: S negated
             case KU: gate_on4<T, KU>(g, h, a, b, c, d, pb); break;
             default: gate_on4<T, KYPH>(g, h, a, b, c, d, pb); break;
             }
