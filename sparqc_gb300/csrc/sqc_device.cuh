@@ -193,12 +193,12 @@ __device__ __forceinline__ float ld_desc(const float* p) {
 #endif
 }
 
-// Programmatic dependent launch. Pass kernels are launched with programmatic stream
+// Programmatic dependent launch. Direct passes are launched with programmatic stream
 // serialization, so the next pass's blocks may be placed on the SMs while the running pass
-// drains. Every pass kernel first waits until the previous grid in the stream has completed
-// and its writes are visible (a no-op without that launch attribute), and then lets the next
-// pass be scheduled: its blocks only wait in turn, and all of this grid's blocks are
-// already resident by then, so nothing waits on a block that cannot be placed.
+// drains. Such a kernel first waits until the previous grid in the stream has completed and
+// its writes are visible (a no-op without that launch attribute), and then lets the next pass
+// be scheduled: its blocks only wait in turn, and all of this grid's blocks are already
+// resident by then, so nothing waits on a block that cannot be placed.
 __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 

@@ -353,8 +353,8 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
 // Every warp is a worker with its own ring of D = RingDepth shared-memory slots. It copies the
 // buckets of the slot D-1 steps ahead with cp.async (one commit group per slot), waits
 // for the current slot's group, moves the slot into registers, applies the gates and writes
-// back in place. A slot holds four buckets: four list entries (stream pass) or two owned
-// pairs (pair pass).
+// back in place. A slot holds the buckets of one item: four list entries (stream pass), two
+// owned pairs (pair pass), one owned quad, or one owned octet (eight buckets).
 constexpr int kWarpsPerBlock = 4;
 constexpr int kStagedThreads = 32 * kWarpsPerBlock;
 // FP32 octet rings hold three slots (two items in flight, 27 KB per block): the same six
