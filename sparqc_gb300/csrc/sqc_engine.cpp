@@ -302,7 +302,7 @@ int Engine::apply(const sqc_gate* gates, uint64_t n) {
 
 // Resolve the queued gates, split the device gates into passes and launch them. A pass is
 // either a run of streamable gates, or one cross-group gate followed by such a run.
-int Engine::flush() {
+int Engine::flush(bool hold_last) {
     if (pending_.empty()) return SQC_OK;
     const size_t n = pending_.size();
     int rc;
@@ -355,6 +355,17 @@ int Engine::flush() {
                      spans.push_back(Span{g0, g1, nx, q1, q2, q3, fixed});
                      encode_pass(hd, g0, g1, q1, q3);
                  });
+    if (hold_last && spans.size() >= 2) {
+        // the last pass's gates, and the host-resolved gates around them, go back to the queue;
+        // the planner returns to its state after the last device gate that is launched
+        const size_t last_src = src[spans.back().g0 - 1];   // log index of that gate
+        const size_t keep = last_src + 1 - log_base;        // queued gates that stay launched
+        pending_.assign(log_.begin() + (std::ptrdiff_t)(log_base + keep), log_.end());
+        log_.resize(log_base + keep);
+        gates_applied_ -= n - keep;
+        plan_ = after[spans.back().g0 - 1];
+        spans.pop_back();
+    }
     if ((rc = cuda(cudaMemcpyAsync(d_desc_ + desc_used_, hd, nd * sizeof(GateDesc), cudaMemcpyHostToDevice, stream_),
                    "H2D gate descriptors")))
         return rc;

@@ -46,7 +46,10 @@ public:
     int set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n,
                   const KeySummary* known = nullptr);
     int apply(const sqc_gate* gates, uint64_t n);
-    int flush();
+    // hold_last: when the queued gates make more than one pass, the last pass is not launched;
+    // its gates stay queued (the planner returns to the state before them), so a caller that
+    // feeds a circuit in slices keeps the passes it would get from the whole circuit.
+    int flush(bool hold_last = false);
     int sync();
     int nnz(uint64_t* out);
     int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);

@@ -283,7 +283,9 @@ int Server::step(uint32_t* finished) {
         g = std::min<uint64_t>(std::max<uint64_t>(8, g), left);
         r.chunk = g;
         if (g && (rc = r.eng->apply(r.gates.data() + r.pos, g))) { err = r.eng->err; return rc; }
-        if ((rc = r.eng->flush())) { err = r.eng->err; return rc; }
+        // a slice that does not end the circuit keeps its last, unfinished pass queued, so the
+        // pass goes on fusing the next slice's gates
+        if ((rc = r.eng->flush(r.pos + g < r.gates.size()))) { err = r.eng->err; return rc; }
     }
     if ((rc = cuda(cudaEventRecord(ev2_, stream_), "event")) || (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
         return rc;
