@@ -59,6 +59,13 @@ int Engine::cuda(cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? SQC_ERR_OOM : SQC_ERR_CUDA;
 }
 
+// A launcher reported a failed launch: its error, or a generic one when the runtime holds none.
+int Engine::launch_failed(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda(e, what);
+    return fail(SQC_ERR_CUDA, std::string(what) + ": launch failed");
+}
+
 size_t Engine::bucket_bytes() const {
     return sizeof(Header) + kSlots * sizeof(unsigned long long) + kSlots * (dbl_ ? 16 : 8) + sizeof(unsigned) +
            sizeof(Unit);
@@ -400,7 +407,7 @@ int Engine::flush(bool hold_last) {
                                            cudaMemcpyHostToDevice, stream_), "H2D tiny passes")))
                 return rc;
             if (launch_tiny(a, d_tiny_ + desc_used_, (uint32_t)spans.size(), dbl_, stream_) < 0)
-                return cuda(cudaGetLastError(), "tiny passes");
+                return launch_failed("tiny passes");
             if (time_passes_) {
                 cudaEvent_t ev = nullptr;
                 if ((rc = record_event(&ev))) return rc;
@@ -432,7 +439,7 @@ int Engine::flush(bool hold_last) {
         if (sp.nx)
             list_hint_ = std::min<unsigned long long>(tab_.nb, std::min(list_hint_ << sp.nx, a.grow_bound));
         const int nl = launch_pass(a, list_hint_, dbl_, sms_, stream_);
-        if (nl < 0) return cuda(cudaGetLastError(), "gate pass");
+        if (nl < 0) return launch_failed("gate pass");
         const bool pair = sp.nx > 0;
         if (time_passes_) {
             cudaEvent_t ev = nullptr;

@@ -87,6 +87,7 @@ public:
 private:
     int fail(int code, const std::string& msg);
     int cuda(cudaError_t e, const char* what);
+    int launch_failed(const char* what);
     size_t bucket_bytes() const;
     int alloc_table(unsigned long long nb, HostTable* out);
     void free_table(HostTable* t);
