@@ -97,7 +97,13 @@ typedef struct sqc_options {
     uint32_t max_cross_qubits; /* qubits >= 4 one pass may pair keys across (branching or swap gates on
                                   them), 1, 2 or 3; 0 = default (3 for FP32, 2 for FP64). Results do
                                   not depend on it. */
-    uint32_t reserved[2];
+    uint32_t device_updates_only; /* 1: sqc_stats.amp_updates counts only gates the device applied;
+                                  0 (default): gates the host resolved without touching the state
+                                  (a known-zero control, an uncontrolled X as a relabelling of the
+                                  keys, a one-sided diagonal gate on a known-zero bit) count too,
+                                  each with the key count it acted on, as in the reference, which
+                                  runs every gate on the device */
+    uint32_t reserved;
 } sqc_options;
 
 typedef struct sqc_state sqc_state;
@@ -203,14 +209,18 @@ int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_er
  * in the caller's DEVICE arrays keys_in/re_in/im_in (n_in distinct keys, at most 16384) and
  * writes the resulting entries, in no particular order, to the caller's DEVICE arrays
  * keys_out/re_out/im_out (capacity cap_out); *n_out (host) receives their number. Same
- * arithmetic, pair rule and pruning as sqc_apply_gates, bit for bit. It calls no
+ * arithmetic and pair rule as sqc_apply_gates, bit for bit, with the pruning of a state created
+ * with the default prune_threshold (1e-14, the only threshold this entry point uses). Keys at or
+ * above 2^nq, or given twice, make the call return SQC_ERR_ARG. It calls no
  * cudaMalloc/cudaFree: the table lives in a fixed device array of about 13 MB, held by every
  * device that loads the library until exit. At most 14745 groups of 16 consecutive keys may
  * have been touched during the call (emptied groups included) when a gate pairing keys across
  * groups runs; beyond that, or when *n_out > cap_out, the call returns SQC_ERR_CAPACITY.
- * Calls share the array: serialize
- * calls whose GPU work could overlap. The first call on a device looks up the array's device
- * address; make it before any stream capture. stream is a cudaStream_t (NULL = default). */
+ * Calls share the array: serialize calls whose GPU work could overlap. The first call on a
+ * device looks up the array's device address and, under CUDA's default lazy module loading,
+ * loads the module that holds it (reserving the array, possibly synchronizing): make it during
+ * initialisation, before any stream capture, or set CUDA_MODULE_LOADING=EAGER.
+ * stream is a cudaStream_t (NULL = default). */
 int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const double* re_in, const double* im_in,
                     uint64_t n_in, const sqc_gate* gates, uint64_t n_gates, uint64_t* keys_out,
                     double* re_out, double* im_out, uint64_t cap_out, uint64_t* n_out, void* stream);
@@ -423,6 +433,11 @@ typedef struct sqc_stats {
 } sqc_stats;
 
 int sqc_get_stats(sqc_state* st, sqc_stats* out);
+/* Device diagnostic (no counterpart in the reference): the FP64 fused multiply-add rate of
+ * device `device`, in lane operations per second, from a timed loop of independent FMA chains
+ * (synchronizes the device; allocates 8 bytes for the duration of the call). On this GPU the
+ * FP64 pipe bounds the FP64 gate passes, and this is its measured peak. */
+int sqc_fp64_rate(uint32_t device, double* fma_per_s);
 const char* sqc_status_string(int status);
 /* Message of the last error on this handle ("" if none). Valid until the next call. */
 const char* sqc_last_error(sqc_state* st);

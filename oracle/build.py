@@ -15,6 +15,7 @@ REF_OUT = os.path.join(HERE, "_ref")
 REFERENCE_ROOT = os.environ.get("SPARQC_REFERENCE_ROOT", "/root/reference")
 
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
+DENSE_SO = os.path.join(BUILD, "libdense.so")
 REFEMU_SO = os.path.join(REF_OUT, "librefemu.so")
 
 
@@ -25,19 +26,29 @@ def _newer(out, srcs):
     return all(os.path.getmtime(s) <= t for s in srcs)
 
 
-def build_oracle(force=False):
-    src = os.path.join(HERE, "sparse_oracle.c")
-    if not force and _newer(ORACLE_SO, [src, __file__]):
-        return ORACLE_SO
+def _build_c(src_name, out, force):
+    src = os.path.join(HERE, src_name)
+    if not force and _newer(out, [src, __file__]):
+        return out
     os.makedirs(BUILD, exist_ok=True)
     base = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-            src, "-o", ORACLE_SO + ".tmp", "-lm"]
+            src, "-o", out + ".tmp", "-lm"]
     try:
         subprocess.run(base[:1] + ["-fopenmp"] + base[1:], check=True, capture_output=True, text=True)
     except subprocess.CalledProcessError:
         subprocess.run(base, check=True, capture_output=True, text=True)
-    os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
-    return ORACLE_SO
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_oracle(force=False):
+    """The sparse restatement of the reference's algorithm (also the CPU baseline)."""
+    return _build_c("sparse_oracle.c", ORACLE_SO, force)
+
+
+def build_dense(force=False):
+    """The paged dense FP64 statevector (textbook matrices, no pruning)."""
+    return _build_c("dense_oracle.c", DENSE_SO, force)
 
 
 def reference_available():

@@ -69,3 +69,91 @@ class DenseOracle:
         nz = ~((np.abs(self.psi.real) < threshold) & (np.abs(self.psi.imag) < threshold))
         keys = np.nonzero(nz)[0].astype(np.uint64)
         return keys, self.psi.real[nz].copy(), self.psi.imag[nz].copy()
+
+
+# ---- paged dense statevector in C (oracle/dense_oracle.c) ---------------------------------
+_dlib = None
+
+
+def _dense_lib():
+    global _dlib
+    if _dlib is None:
+        import ctypes
+        from . import build
+        L = ctypes.CDLL(build.build_dense())
+        P, U64, U32, D, I = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_double, ctypes.c_int
+        L.dno_create.restype = P
+        L.dno_create.argtypes = [I]
+        L.dno_destroy.argtypes = [P]
+        L.dno_set_threads.argtypes = [P, I]
+        L.dno_max_threads.restype = I
+        L.dno_set_state.restype = I
+        L.dno_set_state.argtypes = [P, P, P, P, U64]
+        L.dno_apply1.restype = I
+        L.dno_apply1.argtypes = [P, U32, U64, P]
+        L.dno_apply2.restype = I
+        L.dno_apply2.argtypes = [P, U32, U32, U64, P]
+        L.dno_get_state.restype = U64
+        L.dno_get_state.argtypes = [P, P, P, P, U64, D]
+        _dlib = L
+    return _dlib
+
+
+def _ptr(a):
+    import ctypes
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class PagedDenseOracle:
+    """Dense FP64 statevector of up to 30 qubits (and beyond, for states that reach few pages),
+    starting from |0...0>: the same textbook matrices as DenseOracle, applied in C to every
+    index pair of the full vector; pages that have only held zeros are not stored."""
+
+    def __init__(self, nq, threads=None):
+        if not 1 <= nq <= 40:
+            raise ValueError("nq out of range")
+        self.nq = nq
+        self._L = _dense_lib()
+        self._h = self._L.dno_create(int(nq))
+        if not self._h:
+            raise MemoryError("dno_create failed")
+        self._L.dno_set_threads(self._h, int(threads or self._L.dno_max_threads()))
+
+    def close(self):
+        if self._h:
+            self._L.dno_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, keys, re, im):
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = np.ascontiguousarray(im, dtype=np.float64)
+        if self._L.dno_set_state(self._h, _ptr(keys), _ptr(re), _ptr(im), keys.size):
+            raise ValueError("bad key")
+
+    def apply_matrix(self, targets, controls, m):
+        """Apply a 2x2 (one target) or 4x4 (two targets, index i0 + 2*i1) complex matrix."""
+        m = np.ascontiguousarray(np.asarray(m, dtype=np.complex128)).view(np.float64)
+        if len(targets) == 1:
+            rc = self._L.dno_apply1(self._h, int(targets[0]), int(controls), _ptr(m))
+        else:
+            rc = self._L.dno_apply2(self._h, int(targets[0]), int(targets[1]), int(controls), _ptr(m))
+        if rc:
+            raise ValueError(f"dno_apply failed ({rc})")
+
+    def apply(self, gates):
+        for g in gates:
+            self.apply_matrix([int(g["target"])], int(g["controls"]),
+                              matrix(int(g["kind"]), float(g["theta"]), float(g["phi"]), float(g["lambda"])))
+
+    def state(self, threshold=1e-14):
+        """Key-sorted entries whose amplitude is not negligible (|re|,|im| < threshold)."""
+        n = int(self._L.dno_get_state(self._h, None, None, None, 0, threshold))
+        keys = np.empty(n, np.uint64)
+        re = np.empty(n, np.float64)
+        im = np.empty(n, np.float64)
+        self._L.dno_get_state(self._h, _ptr(keys), _ptr(re), _ptr(im), n, threshold)
+        return keys, re, im

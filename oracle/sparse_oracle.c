@@ -55,6 +55,10 @@ typedef struct {
     uint64_t *idx;      /* position+1, 0 = empty */
     int nthreads;
     uint64_t amp_updates;  /* sum over applied gates of the input key count */
+    uint64_t scap;         /* scratch entries allocated */
+    uint64_t *sk;          /* scratch: output keys, values and validity of a key-changing gate */
+    double *sr, *si;
+    unsigned char *sv;
 } orc_state;
 
 typedef struct { double c, s; double m[8]; } coef_t;
@@ -180,7 +184,9 @@ static int build_index(orc_state* st) {
         if (!st->idx) { st->icap = 0; return -1; }
         st->icap = want;
     }
-    memset(st->idx, 0, st->icap * sizeof(uint64_t));
+    const int64_t ic = (int64_t)st->icap;
+#pragma omp parallel for schedule(static) num_threads(st->nthreads)
+    for (int64_t i = 0; i < ic; ++i) st->idx[i] = 0;
     const uint64_t mask = st->icap - 1;
     const int64_t n = (int64_t)st->n;
 #pragma omp parallel for schedule(static) num_threads(st->nthreads)
@@ -237,7 +243,8 @@ orc_state* orc_create(int precision, double prune_threshold) {
 
 void orc_destroy(orc_state* st) {
     if (!st) return;
-    free(st->keys); free(st->re); free(st->im); free(st->idx); free(st);
+    free(st->keys); free(st->re); free(st->im); free(st->idx);
+    free(st->sk); free(st->sr); free(st->si); free(st->sv); free(st);
 }
 
 void orc_set_threads(orc_state* st, int nthreads) { st->nthreads = nthreads > 0 ? nthreads : 1; }
@@ -265,7 +272,35 @@ int orc_set_state(orc_state* st, const uint64_t* keys, const double* re, const d
     return 0;
 }
 
-/* Apply one gate: every pair with at least one present member is updated once. */
+/* Output scratch of a key-changing gate, kept between gates (2n entries). */
+static int scratch(orc_state* st, uint64_t n2) {
+    if (n2 <= st->scap) return 0;
+    free(st->sk); free(st->sr); free(st->si); free(st->sv);
+    st->sk = (uint64_t*)malloc(n2 * sizeof(uint64_t));
+    st->sr = (double*)malloc(n2 * sizeof(double));
+    st->si = (double*)malloc(n2 * sizeof(double));
+    st->sv = (unsigned char*)malloc(n2);
+    if (!st->sk || !st->sr || !st->si || !st->sv) { st->scap = 0; return -1; }
+    st->scap = n2;
+    return 0;
+}
+
+/* The 2x2 update of one pair at the state's precision. */
+static inline void pair_any(const orc_state* st, uint32_t kind, const coef_t* k, double v0r, double v0i,
+                            double v1r, double v1i, double* o0r, double* o0i, double* o1r, double* o1i) {
+    if (st->prec == 32) {
+        float a, b, c2, d;
+        pair32(kind, k, (float)v0r, (float)v0i, (float)v1r, (float)v1i, &a, &b, &c2, &d);
+        *o0r = a; *o0i = b; *o1r = c2; *o1i = d;
+    } else {
+        pair64(kind, k, v0r, v0i, v1r, v1i, o0r, o0i, o1r, o1i);
+    }
+}
+
+/* Apply one gate: every pair with at least one present member is updated once.
+ * A diagonal gate's outputs each depend on their own input only and it keeps every key
+ * (emulator/device/device_data.cuh:108-131), so it is applied in place, key by key, with the
+ * same pair formula and no index rebuild. */
 static int apply_one(orc_state* st, const orc_gate* g) {
     if (g->kind >= K_COUNT || g->target > 63) return -3;
     const uint64_t bq = 1ULL << g->target;
@@ -275,15 +310,32 @@ static int apply_one(orc_state* st, const orc_gate* g) {
     const int cls = gate_class(g->kind);
     const uint64_t C = g->controls;
     const int64_t n = (int64_t)st->n;
-    uint64_t* ok = (uint64_t*)malloc(2 * (size_t)n * sizeof(uint64_t) + 1);
-    double* orr = (double*)malloc(2 * (size_t)n * sizeof(double) + 1);
-    double* oi = (double*)malloc(2 * (size_t)n * sizeof(double) + 1);
-    unsigned char* valid = (unsigned char*)calloc(2 * (size_t)n + 1, 1);
-    if (!ok || !orr || !oi || !valid) { free(ok); free(orr); free(oi); free(valid); return -1; }
+    if (cls == C_DIAG) {
+#pragma omp parallel for schedule(static) num_threads(st->nthreads)
+        for (int64_t i = 0; i < n; ++i) {
+            const uint64_t key = st->keys[i];
+            if ((key & C) != C) continue;
+            double o0r, o0i, o1r, o1i;
+            if (key & bq) {
+                pair_any(st, g->kind, &k, 0., 0., st->re[i], st->im[i], &o0r, &o0i, &o1r, &o1i);
+                st->re[i] = o1r; st->im[i] = o1i;
+            } else {
+                pair_any(st, g->kind, &k, st->re[i], st->im[i], 0., 0., &o0r, &o0i, &o1r, &o1i);
+                st->re[i] = o0r; st->im[i] = o0i;
+            }
+        }
+        return 0;
+    }
+    if (scratch(st, 2 * (uint64_t)n + 1)) return -1;
+    uint64_t* ok = st->sk;
+    double* orr = st->sr;
+    double* oi = st->si;
+    unsigned char* valid = st->sv;
 
 #pragma omp parallel for schedule(static) num_threads(st->nthreads)
     for (int64_t i = 0; i < n; ++i) {
         const uint64_t key = st->keys[i];
+        valid[2 * i] = valid[2 * i + 1] = 0;
         if ((key & C) != C) {            /* control not satisfied: the key passes unchanged */
             ok[2 * i] = key; orr[2 * i] = st->re[i]; oi[2 * i] = st->im[i]; valid[2 * i] = 1;
             continue;
@@ -302,28 +354,38 @@ static int apply_one(orc_state* st, const orc_gate* g) {
             have1 = 1; v1r = st->re[i]; v1i = st->im[i];
         }
         double o0r, o0i, o1r, o1i;
-        if (st->prec == 32) {
-            float a, b, c2, d;
-            pair32(g->kind, &k, (float)v0r, (float)v0i, (float)v1r, (float)v1i, &a, &b, &c2, &d);
-            o0r = a; o0i = b; o1r = c2; o1i = d;
-        } else {
-            pair64(g->kind, &k, v0r, v0i, v1r, v1i, &o0r, &o0i, &o1r, &o1i);
-        }
+        pair_any(st, g->kind, &k, v0r, v0i, v1r, v1i, &o0r, &o0i, &o1r, &o1i);
         int e0, e1;
         if (cls == C_SWAP) { e0 = have1; e1 = have0; }
-        else if (cls == C_DIAG) { e0 = have0; e1 = have1; }
         else { e0 = !negligible(o0r, o0i, st->thr); e1 = !negligible(o1r, o1i, st->thr); }
         if (e0) { ok[2 * i] = k0; orr[2 * i] = o0r; oi[2 * i] = o0i; valid[2 * i] = 1; }
         if (e1) { ok[2 * i + 1] = k1; orr[2 * i + 1] = o1r; oi[2 * i + 1] = o1i; valid[2 * i + 1] = 1; }
     }
-    uint64_t m = 0;
-    for (int64_t i = 0; i < 2 * n; ++i) m += valid[i];
-    if (reserve(st, m > 16 ? m : 16)) { free(ok); free(orr); free(oi); free(valid); return -1; }
-    uint64_t w = 0;
-    for (int64_t i = 0; i < 2 * n; ++i)
-        if (valid[i]) { st->keys[w] = ok[i]; st->re[w] = orr[i]; st->im[w] = oi[i]; ++w; }
-    st->n = w;
-    free(ok); free(orr); free(oi); free(valid);
+    /* stable compaction of the valid outputs: per-thread counts over fixed ranges, a prefix sum,
+     * then each range copies its entries to its offset (the same order as one serial sweep) */
+    enum { kParts = 256 };
+    uint64_t cnt[kParts + 1];
+    const int64_t m2 = 2 * n;
+    const int64_t per = (m2 + kParts - 1) / kParts;
+#pragma omp parallel for schedule(static) num_threads(st->nthreads)
+    for (int p = 0; p < kParts; ++p) {
+        uint64_t c = 0;
+        const int64_t lo = (int64_t)p * per, hi = lo + per < m2 ? lo + per : m2;
+        for (int64_t i = lo; i < hi; ++i) c += valid[i];
+        cnt[p + 1] = c;
+    }
+    cnt[0] = 0;
+    for (int p = 0; p < kParts; ++p) cnt[p + 1] += cnt[p];
+    const uint64_t m = cnt[kParts];
+    if (reserve(st, m > 16 ? m : 16)) return -1;
+#pragma omp parallel for schedule(static) num_threads(st->nthreads)
+    for (int p = 0; p < kParts; ++p) {
+        uint64_t w = cnt[p];
+        const int64_t lo = (int64_t)p * per, hi = lo + per < m2 ? lo + per : m2;
+        for (int64_t i = lo; i < hi; ++i)
+            if (valid[i]) { st->keys[w] = ok[i]; st->re[w] = orr[i]; st->im[w] = oi[i]; ++w; }
+    }
+    st->n = m;
     return build_index(st);
 }
 

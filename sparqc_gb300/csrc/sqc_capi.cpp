@@ -6,6 +6,7 @@
 
 #include "../../include/sparqc.h"
 #include "sqc_handles.h"
+#include "sqc_kernels.h"
 
 namespace {
 
@@ -49,7 +50,8 @@ void sqc_default_options(sqc_options* opt) {
     opt->max_fused_gates = 0;
     opt->time_passes = 0;
     opt->max_cross_qubits = 0;
-    for (int i = 0; i < 2; ++i) opt->reserved[i] = 0;
+    opt->device_updates_only = 0;
+    opt->reserved = 0;
 }
 
 int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt, sqc_state** out) {
@@ -168,6 +170,21 @@ int sqc_sample(sqc_state* st, uint64_t shots, uint64_t seed, uint64_t* keys) {
 int sqc_get_stats(sqc_state* st, sqc_stats* out) {
     if (!out) return SQC_ERR_ARG;
     return guarded(st, [&](sqc::Engine& e) { return e.stats(out); });
+}
+
+int sqc_fp64_rate(uint32_t device, double* fma_per_s) {
+    if (!fma_per_s) return SQC_ERR_ARG;
+    *fma_per_s = 0.0;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || (int)device >= ndev) return SQC_ERR_NO_DEVICE;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice((int)device) != cudaSuccess) return SQC_ERR_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, (int)device);
+    const cudaError_t e = sqc::measure_fp64_rate(sms, fma_per_s);
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? SQC_OK : SQC_ERR_CUDA;
 }
 
 const char* sqc_status_string(int status) {

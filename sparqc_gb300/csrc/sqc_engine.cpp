@@ -98,6 +98,7 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     // occupancy and it ran 10% slower)
     max_nx_ = o.max_cross_qubits ? o.max_cross_qubits : (o.precision == SQC_FP32 ? 3 : 2);
     time_passes_ = o.time_passes != 0;
+    dev_upd_only_ = o.device_updates_only != 0;
     device_ = (int)o.device;
 
     int ndev = 0;
@@ -334,7 +335,7 @@ int Engine::flush(bool hold_last) {
     for (size_t i = 0; i < n; ++i) {
         GateDesc d;
         if (!plan_gate(pending_[i], &d)) continue;
-        d.pad = plan_.credit;
+        d.pad = dev_upd_only_ ? 0u : plan_.credit;   // credit: host-resolved gates before it
         plan_.credit = 0;
         hd[nd++] = d;
         src.push_back(log_base + i);
@@ -514,7 +515,7 @@ int Engine::sync() {
         if ((rc = read_ctl())) return rc;
         const unsigned st = ctl_host_->status;
         if (st == ST_OK) {
-            host_upd_ += (unsigned long long)plan_.credit * ctl_host_->nnz;
+            if (!dev_upd_only_) host_upd_ += (unsigned long long)plan_.credit * ctl_host_->nnz;
             plan_.credit = 0;
             seq_verified_ = ctl_host_->seq;
             log_.clear();

@@ -109,6 +109,7 @@ private:
     uint32_t nq_ = 0;
     bool dbl_ = true;
     double thr_ = 1e-14;
+    bool dev_upd_only_ = false;     // amp updates count device-applied gates only
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
     uint32_t max_nx_ = 2;        // cross-group qubits per pass at most (3: direct-kernel tables only)

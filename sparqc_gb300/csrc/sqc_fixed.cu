@@ -6,9 +6,15 @@
 // device must not be disturbed by a cudaMalloc/cudaFree, which synchronizes the device).
 // This entry point serves them. The caller passes its sparse state and receives the result
 // in device arrays it owns; the hash table, its control block and the gate descriptors live
-// in one file-scope device array of fixed size, reserved when the library is loaded and
-// held by every device that loads it until the process exits.
+// in one file-scope device array of fixed size, held by every device that loads it until the
+// process exits. With CUDA's lazy module loading (the default) the module holding the array is
+// loaded on a device by the first call made there, which then reserves the array (about 13 MB)
+// and may synchronize: make that first call during initialisation, or load modules eagerly
+// (CUDA_MODULE_LOADING=EAGER).
 //
+// Pruning uses the engine's default threshold, 1e-14: results equal sqc_apply_gates' for states
+// created with the default prune_threshold. Input keys must lie below 2^nq and be distinct
+// (SQC_ERR_ARG otherwise).
 // Limits: FP64 amplitudes; at most kFixedMaxInput input keys and kFixedMaxGates gates per
 // call; at most 14745 (= 0.45 * kFixedBuckets) groups of 16 consecutive keys may have been
 // touched when a gate that pairs keys across groups runs (branching or X/Y gates on qubits
@@ -23,6 +29,7 @@
 // the array: serialize them. The device address of the array is looked up once per device
 // (cudaGetSymbolAddress, with that device current) on the first call made on it; make that
 // first call before any stream capture.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -75,41 +82,19 @@ cudaError_t fixed_base(int dev, void** out, int* sms) {
 
 bool diag_kind(uint32_t k) { return k == KZ || k == KPHASE || k == KRZ || k == KS || k == KSDG || k == KT || k == KTDG; }
 
-// Gate descriptor with host-resolved coefficients, identity key frame.
-void describe(const sqc_gate& g, GateDesc* d) {
-    std::memset(d, 0, sizeof *d);
-    d->kind = g.kind;
-    d->target = g.target;
-    d->ctrl = g.controls;
-    d->cval = g.controls;
-    switch (g.kind) {
-    case KPHASE: d->c = std::cos(g.theta); d->s = std::sin(g.theta); break;
-    case KRZ: case KRX: case KRY: {
-        const double h = g.theta / 2.;
-        d->c = std::cos(h);
-        d->s = std::sin(h);
-        break;
-    }
-    case KT: d->c = 0.70710678118654752440; d->s = 0.70710678118654752440; break;
-    case KTDG: d->c = 0.70710678118654752440; d->s = -0.70710678118654752440; break;
-    case KH: d->c = 1. / std::sqrt(2.); break;
-    case KU: {
-        const double c = std::cos(g.theta / 2.), s = std::sin(g.theta / 2.);
-        const double cl = std::cos(g.lambda), sl = std::sin(g.lambda);
-        const double cp = std::cos(g.phi), sp = std::sin(g.phi);
-        const double cpl = std::cos(g.phi + g.lambda), spl = std::sin(g.phi + g.lambda);
-        d->m[0] = c;         d->m[1] = 0.;
-        d->m[2] = -(cl * s); d->m[3] = -(sl * s);
-        d->m[4] = cp * s;    d->m[5] = sp * s;
-        d->m[6] = cpl * c;   d->m[7] = spl * c;
-        break;
-    }
-    default: break;
-    }
-    d->cf = (float)d->c;
-    d->sf = (float)d->s;
-    for (int i = 0; i < 8; ++i) d->mf[i] = (float)d->m[i];
+// Keys with a bit at or above nq are not states of the register: flag them (ST_BAD_KEY).
+__global__ void fixed_key_check_kernel(const unsigned long long* __restrict__ keys, unsigned long long n,
+                                       unsigned long long outside, Ctl* ctl) {
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        if (keys[i] & outside) atomicCAS(&ctl->status, 0u, (unsigned)ST_BAD_KEY);
 }
+
+// Calls made on each device since its scratch headers were last cleared. Every call bumps the
+// table epoch once; before the 32-bit epoch could come back to a value stale headers hold, the
+// headers and the control block are cleared (cudaMemsetAsync allocates nothing).
+unsigned long long g_fixed_calls[kMaxDevices] = {};
+constexpr unsigned long long kEpochRestart = 0xFFFFFF00ULL;
 
 }  // namespace
 }  // namespace sqc
@@ -127,10 +112,8 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     GateDesc hd[kFixedMaxGates];
     for (uint64_t i = 0; i < n_gates; ++i) {
         const sqc_gate& g = gates[i];
-        if (g.kind > SQC_U || g.target >= nq) return SQC_ERR_ARG;
-        if (nq < 64 && (g.controls >> nq)) return SQC_ERR_ARG;
-        if ((g.controls >> g.target) & 1ULL) return SQC_ERR_ARG;
-        describe(g, &hd[i]);
+        if (check_gate(g, nq)) return SQC_ERR_ARG;
+        hd[i] = make_desc(Planner{}, g.kind, g.target, g.controls, g);   // identity key frame
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SQC_ERR_NO_DEVICE;
@@ -149,10 +132,26 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     GateDesc* d_desc = reinterpret_cast<GateDesc*>(b + kOffDesc);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
+    {
+        std::lock_guard<std::mutex> lock(g_fixed_mu);
+        if (++g_fixed_calls[dev] >= kEpochRestart) {
+            if (cudaMemsetAsync(t.hdr, 0, kFixedBuckets * sizeof(Header), st) != cudaSuccess ||
+                cudaMemsetAsync(ctl, 0, sizeof(Ctl), st) != cudaSuccess)
+                return SQC_ERR_CUDA;
+            g_fixed_calls[dev] = 1;
+        }
+    }
     // load the caller's state (the kernels read its device arrays; the epoch bump frees the table)
     if (launch_set_state(reinterpret_cast<const unsigned long long*>(keys_in), re_in, im_in, n_in, t, ctl, true,
                          sms, st) != cudaSuccess)
         return SQC_ERR_CUDA;
+    if (nq < 64 && n_in) {
+        const unsigned long long outside = ~((1ULL << nq) - 1);
+        const int grid = (int)std::min<unsigned long long>((n_in + 255) / 256, (unsigned long long)sms * 4);
+        fixed_key_check_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const unsigned long long*>(keys_in), n_in,
+                                                     outside, ctl);
+        if (cudaGetLastError() != cudaSuccess) return SQC_ERR_CUDA;
+    }
     // same pass split as the engine with one cross-group qubit per pass: one cross-group gate,
     // then a stream run; each pass's gates are encoded before the descriptors are uploaded
     struct Span {
@@ -206,7 +205,7 @@ extern "C" int sqc_apply_fixed(uint32_t nq, const uint64_t* keys_in, const doubl
     if (cudaMemcpyAsync(&c, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return SQC_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return SQC_ERR_CUDA;
     if (c.status == ST_GROW || c.status == ST_TABLE_FULL) return SQC_ERR_CAPACITY;
-    if (c.status == ST_DUPLICATE) return SQC_ERR_ARG;
+    if (c.status == ST_DUPLICATE || c.status == ST_BAD_KEY) return SQC_ERR_ARG;
     if (c.status != ST_OK) return SQC_ERR_STATE;
     *n_out = c.out_count;
     return c.out_count > cap_out ? SQC_ERR_CAPACITY : SQC_OK;

@@ -418,6 +418,48 @@ cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long
     return cudaGetLastError();
 }
 
+// Throughput probe of the FP64 pipe: every thread runs eight independent chains of dependent
+// fused multiply-adds (x = x * a + b), so the pipe, not latency, bounds it. The result is kept
+// alive by a store no input can trigger.
+__global__ void fp64_rate_kernel(double* sink, double a, double b, int iters) {
+    double x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = __fma_rn(x[k], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == -1.0) sink[0] = s;
+}
+
+cudaError_t measure_fp64_rate(int sms, double* fma_per_s) {
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc(&sink, sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {   // the first launch warms up
+        cudaEventRecord(e0);
+        fp64_rate_kernel<<<blocks, threads>>>(sink, 0.9999999, 1e-7, iters);
+        cudaEventRecord(e1);
+        e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (sink) cudaFree(sink);
+    *fma_per_s = (e == cudaSuccess && best > 0.f) ? (double)blocks * threads * iters * 8 / (best * 1e-3) : 0.0;
+    return e;
+}
+
 cudaError_t launch_rehash(const TableDev& told, unsigned long long n_old, const TableDev& tnew, unsigned ep_new,
                           int amp_bytes, Ctl* ctl, int sms, cudaStream_t st) {
     const int grid = grid_for(n_old / 2 + 1, kThreads / 32, sms);

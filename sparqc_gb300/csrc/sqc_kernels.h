@@ -33,6 +33,9 @@ cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hin
 cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,
                            const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
                            unsigned long long d, Ctl* out, int sms, cudaStream_t st);
+// Measured FP64 fused multiply-add rate of the current device (lane operations per second), from
+// a timed loop of independent FMA chains over sms * 8 blocks. Synchronizes the device.
+cudaError_t measure_fp64_rate(int sms, double* fma_per_s);
 cudaError_t launch_rehash(const TableDev& told, unsigned long long n_old, const TableDev& tnew, unsigned ep_new,
                           int amp_bytes, Ctl* ctl, int sms, cudaStream_t st);
 

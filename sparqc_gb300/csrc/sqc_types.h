@@ -16,7 +16,8 @@ enum Status : unsigned int {
     ST_TABLE_FULL = 1,   // a claim found no free bucket within kMaxProbe (state no longer valid)
     ST_DUPLICATE = 2,    // set_state saw the same key twice
     ST_GROW = 3,         // a pair pass refused to start: the table might overflow (state intact)
-    ST_TIMEOUT = 4       // a bounded wait inside a pass ran out (state no longer valid)
+    ST_TIMEOUT = 4,      // a bounded wait inside a pass ran out (state no longer valid)
+    ST_BAD_KEY = 5       // a loaded key has a bit at or above the register's qubit count
 };
 
 // gate kinds (0..12 = sqc_gate.kind); KYPH is internal: the diagonal left over when an

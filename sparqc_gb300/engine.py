@@ -23,7 +23,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
            "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
-           "sqc_load",
+           "sqc_load", "sqc_fp64_rate",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_get_states",
@@ -47,7 +47,8 @@ class Options(ctypes.Structure):
                 ("load_factor", ctypes.c_double), ("initial_buckets", ctypes.c_uint64),
                 ("stream", ctypes.c_void_p), ("device", ctypes.c_uint32),
                 ("max_fused_gates", ctypes.c_uint32), ("time_passes", ctypes.c_uint32),
-                ("max_cross_qubits", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("max_cross_qubits", ctypes.c_uint32), ("device_updates_only", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -157,6 +158,8 @@ def load(path=LIB_PATH):
     L.sqc_last_error.restype = ctypes.c_char_p
     L.sqc_stream.argtypes = [P]
     L.sqc_stream.restype = P
+    L.sqc_fp64_rate.argtypes = [U32, ctypes.POINTER(D)]
+    L.sqc_fp64_rate.restype = I
     L.sqc_batch_default_options.argtypes = [ctypes.POINTER(BatchOptions)]
     L.sqc_batch_default_options.restype = None
     L.sqc_batch_create.argtypes = [ctypes.POINTER(BatchOptions), ctypes.POINTER(P)]
@@ -229,11 +232,22 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def fp64_rate(device=0):
+    """Measured FP64 fused multiply-add rate of a device (lane operations per second)."""
+    L = load()
+    r = ctypes.c_double()
+    rc = L.sqc_fp64_rate(device, ctypes.byref(r))
+    if rc != OK:
+        raise SparqcError(rc, f"sqc_fp64_rate: {L.sqc_status_string(rc).decode()}")
+    return r.value
+
+
 class State:
     """A sparse statevector of ``nq`` qubits on one GPU, starting in |0...0>."""
 
     def __init__(self, nq, precision=FP64, prune_threshold=1e-14, load_factor=0.5, initial_buckets=0,
-                 stream=None, device=0, max_fused_gates=0, params=None, time_passes=False, max_cross_qubits=0):
+                 stream=None, device=0, max_fused_gates=0, params=None, time_passes=False, max_cross_qubits=0,
+                 device_updates_only=False):
         self._L = load()
         o = Options()
         self._L.sqc_default_options(ctypes.byref(o))
@@ -246,6 +260,7 @@ class State:
         o.max_fused_gates = max_fused_gates
         o.time_passes = 1 if time_passes else 0
         o.max_cross_qubits = max_cross_qubits
+        o.device_updates_only = 1 if device_updates_only else 0
         h = ctypes.c_void_p()
         pp = ctypes.byref(params) if params is not None else None
         rc = self._L.sqc_create(nq, pp, ctypes.byref(o), ctypes.byref(h))

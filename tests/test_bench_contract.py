@@ -1,7 +1,7 @@
 """bench.py keeps its JSON contract: one line with the metric, the timing keys, the end-to-end
 number, the roofline of the dominant kernel, the CPU baseline and the launch count.
 
-Runs bench.py itself (on a reduced 40-qubit case and a small batch) on the GPU.
+Runs bench.py itself (on a reduced 64-qubit case and a small batch) on the GPU.
 """
 import json
 import os
@@ -42,7 +42,14 @@ def test_single_state_line():
     assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-12
     cb = d["cpu_baseline"]
     assert cb["value"] > 0 and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert cb["single_thread"]["value"] > 0 and cb["single_thread"]["cores"] == 1 and cb["cpu"]
     assert d["gpu_launches"] > 0
+    assert d["config"]["workload"].startswith("c3") and d["config"]["qubits"] == 64
+    du = d["device_amp_updates"]
+    assert 0 < du["per_step"] <= du["all_gates_per_step"] and du["value"] <= d["value"]
+    assert rf["fp64_pipe"]["peak_fma_lane_ops_per_s"] > 1e11
+    f32 = d["fp32"]
+    assert f32["value"] > 0 and f32["dtype"] == "f32" and f32["fidelity_vs_fp64"] >= 1 - 1e-6
 
 
 @pytest.mark.gpu

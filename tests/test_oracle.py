@@ -174,3 +174,32 @@ def test_reference_rxry_race_breaks_its_address_book():
     o = SparseOracle()
     o.apply(g)
     assert o.nnz == 16 and o.norm2() == pytest.approx(1.0, abs=1e-13)
+
+
+ALL_KINDS = ((G.Z, G.S, G.SDG, G.T, G.TDG, G.RZ, G.PHASE), (G.X, G.Y), (G.H, G.RX, G.RY, G.U))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_paged_dense_equals_numpy_dense(seed):
+    """The paged C statevector applies the same textbook matrices as the numpy one."""
+    from oracle.dense import PagedDenseOracle
+    rng = circuits.SplitMix64(circuits.stream_seed("paged", seed))
+    g = circuits.random_circuit(13, 9, 200, 3, rng, kinds=ALL_KINDS)
+    a = DenseOracle(13)
+    a.apply(g)
+    b = PagedDenseOracle(13)
+    b.apply(g)
+    assert_close(b.state(), a.state(), rel=1e-13, floor=1e-15)
+
+
+def test_paged_dense_30_qubits_against_sparse():
+    """A 30-qubit circuit of the batching configuration's kind: the dense statevector and the
+    sparse restatement agree within the tolerance (the latter prunes at 1e-14)."""
+    from oracle.dense import PagedDenseOracle
+    rng = circuits.SplitMix64(circuits.stream_seed("paged30"))
+    g = circuits.random_circuit(30, 14, 400, 3, rng)
+    d = PagedDenseOracle(30)
+    d.apply(g)
+    o = SparseOracle(threads=SparseOracle.max_threads())
+    o.apply(g)
+    assert_close(drop_negligible(o.state()), d.state())

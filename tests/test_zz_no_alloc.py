@@ -11,8 +11,9 @@ import ctypes
 import numpy as np
 import pytest
 
+from oracle.sparse import SparseOracle
 from sparqc_gb300 import circuits, gates as G
-from sparqc_gb300.engine import ERR_CAPACITY, OK, State, load
+from sparqc_gb300.engine import ERR_ARG, ERR_CAPACITY, OK, State, load
 
 pytestmark = pytest.mark.gpu
 
@@ -69,16 +70,48 @@ def _case(seed, nq, k, depth):
     return keys, re / norm, im / norm, gates
 
 
+def _oracle(keys, re, im, gates):
+    o = SparseOracle()
+    o.set_state(keys, re, im)
+    o.apply(gates)
+    return o.state(sorted=True)
+
+
 def test_fixed_matches_allocating_path_call_after_call():
-    # two calls in a row on the shared scratch, both within the fixed table's group limit
+    # two calls in a row on the shared scratch, both within the fixed table's group limit; each
+    # result also equals the oracle's (the reference's algorithm restated on the CPU)
     for seed, nq, k, depth in ((1, 40, 10, 200), (2, 64, 12, 100)):
         keys, re, im, gates = _case(seed, nq, k, depth)
         rc, fk, fr, fi = _fixed(nq, keys, re, im, gates, 1 << 18)
         assert rc == OK
         want = _allocating(nq, keys, re, im, gates)
         assert fk.size > 0
-        for x, y in zip((fk, fr, fi), want):
-            assert np.array_equal(x, y)
+        for x, y, z in zip((fk, fr, fi), want, _oracle(keys, re, im, gates)):
+            assert np.array_equal(x, y) and np.array_equal(x, z)
+
+
+def test_fixed_rejects_keys_outside_the_register_and_duplicates():
+    z = np.zeros(2)
+    gates = G.gate_array([(G.H, 0)])
+    rc, *_ = _fixed(20, np.array([3, 1 << 20], np.uint64), z + 0.5, z + 0.5, gates, 16)
+    assert rc == ERR_ARG
+    rc, *_ = _fixed(20, np.array([7, 7], np.uint64), z + 0.5, z + 0.5, gates, 16)
+    assert rc == ERR_ARG
+
+
+def test_fixed_capacity_refusal_then_a_clean_call():
+    # 16000 keys in distinct 16-key groups, then H on qubit 4: the pass could need 32000 groups,
+    # more than the fixed table takes, and refuses before touching anything
+    keys = (np.arange(16000, dtype=np.uint64) << np.uint64(5))
+    re = np.full(keys.size, 1.0 / np.sqrt(keys.size))
+    rc, *_ = _fixed(30, keys, re, np.zeros(keys.size), G.gate_array([(G.H, 4)]), 1 << 16)
+    assert rc == ERR_CAPACITY
+    # the next call on the same scratch is unaffected
+    keys, re, im, gates = _case(1, 40, 10, 200)
+    rc, fk, fr, fi = _fixed(40, keys, re, im, gates, 1 << 18)
+    assert rc == OK
+    for x, y in zip((fk, fr, fi), _allocating(40, keys, re, im, gates)):
+        assert np.array_equal(x, y)
 
 
 def test_fixed_rejects_oversized_input():
