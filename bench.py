@@ -1,21 +1,27 @@
 #!/usr/bin/env python
 """Benchmark of the sparse statevector gate path: amp-updates/s on one GB300.
 
-Workload (default): the 40-qubit configuration -- a seeded 2000-gate circuit from |0...0>,
-H on qubits 0..19 then 30% diagonal / 30% permutation / 40% branching gates with 0-3
-controls, branching targets < 20 (at most 2^20 nonzeros), FP64 amplitudes, table load
-factor 0.5. One step = the whole circuit from |0...0>. Synthetic data: the reference
-publishes no benchmark circuits.
+Workload (default): the 64-qubit configuration, the largest that fits one GPU -- a seeded
+500-gate circuit from |0...0>, H on qubits 0..25 then 30% diagonal / 30% permutation / 40%
+branching gates with 0-3 controls, branching targets < 26 (at most 2^26 nonzeros), FP64
+amplitudes, table load factor 0.5; the same circuit in FP32 amplitudes is reported beside it
+("fp32"). One step = the whole circuit from |0...0>. Synthetic data: the reference publishes no
+benchmark circuits. --workload c1/c2 select the 20- and 40-qubit configurations, c4 the
+256-circuit batch, c5 the served Poisson stream.
 
 value   : sum over gates of input nonzeros / device time (CUDA events on the engine's
-          stream, inputs resident, L2 flushed before every step).
+          stream, inputs resident, L2 flushed before every step). Gates the host resolves
+          without touching the state count, as they do in the reference (which runs every gate
+          on the device); "device_amp_updates" counts the device-applied gates alone.
 e2e     : the same metric through the C ABI with host buffers: gate array host->device,
           state |0...0>, every gate, the final state read back to host arrays.
 roofline: the gate-pass kernel; achieved = algorithmic bytes of the passes (device
           counter, see sqc_stats.alg_bytes) / their measured time; peak = the measured
-          HBM copy bandwidth.
+          HBM copy bandwidth. "fp64_pipe" adds the FP64 fused multiply-add rate measured
+          here (sqc_fp64_rate) and the pipe activity of the committed ncu capture.
 cpu_baseline / --impl reference: the CPU restatement of the reference algorithm
-          (oracle/sparse_oracle.c, OpenMP over nonzeros) on a bounded prefix of the circuit.
+          (oracle/sparse_oracle.c, OpenMP over nonzeros) on a bounded prefix of the circuit,
+          on every host core and on one.
 
 Multi-GPU: independent replicas (one circuit per rank, different seeds), no collective on
 the data path; value = all ranks' amp-updates / the slowest rank's time ("weak").
@@ -42,7 +48,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="sparqc", choices=["sparqc", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--no-fp32", action="store_true", help="c1-c3 FP64: skip the FP32 run of the same circuit")
     ap.add_argument("--circuits", type=int, default=256, help="c4: circuits per batch")
     ap.add_argument("--autotune", action="store_true", help="c4: autotune the batch before timing")
     ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
@@ -104,13 +111,36 @@ def cpu_run(gates, seconds, threads, precision):
     return o.amp_updates, dt, n
 
 
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                name = line.split(":", 1)[1].strip()
+                if name:
+                    break
+        else:
+            name = ""
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+        return f"{name} ({os.cpu_count()} cores)"
+    except Exception:
+        return f"{os.cpu_count()} cores"
+
+
 def cpu_baseline(gates, seconds, precision):
+    """The oracle port on every host core, and on one (a bounded prefix of the circuit each)."""
     from oracle.sparse import SparseOracle
     threads = max(1, SparseOracle.max_threads())
     upd, dt, n = cpu_run(gates, seconds, threads, precision)
+    upd1, dt1, n1 = cpu_run(gates, seconds, 1, precision)
     return {"value": upd / dt, "unit": "amp-updates/s", "cores": threads, "kind": "port",
             "sample": f"first {n} of {gates.size} gates ({upd:.3e} amp-updates in {dt:.1f} s), "
-                      f"oracle/sparse_oracle.c, {threads} OpenMP threads"}
+                      f"oracle/sparse_oracle.c, {threads} OpenMP threads",
+            "cpu": cpu_model(),
+            "single_thread": {"value": upd1 / dt1, "unit": "amp-updates/s", "cores": 1,
+                              "sample": f"first {n1} of {gates.size} gates ({upd1:.3e} amp-updates in {dt1:.1f} s)"}}
 
 
 # --------------------------------------------------------------------------------------
@@ -167,18 +197,37 @@ class ClockSampler:
 
 
 def read_profile(name):
-    """Key: value lines of a committed ncu summary (profiles/<name>.txt), {} if absent."""
+    """Key: value lines of a committed ncu summary (profiles/<name>.txt), {} if absent. Numeric
+    values become floats; the command, the capture and the commit it was taken at stay text."""
     out = {}
     try:
         for line in open(os.path.join(PROFILES, name + ".txt")):
             if ":" in line and not line.startswith((" ", "#")):
                 k, v = line.split(":", 1)
+                k, v = k.strip(), v.strip()
+                if k in ("command", "captured", "commit"):
+                    out[k] = v
+                    continue
                 try:
-                    out[k.strip()] = float(v.strip().split()[0])
+                    out[k] = float(v.split()[0])
                 except (ValueError, IndexError):
                     pass
     except OSError:
         pass
+    return out
+
+
+def profile_block(prof, name):
+    """The committed ncu summary's figures, labelled as such: they come from a separate capture
+    (the command and commit it records), not from this run."""
+    if not prof:
+        return None
+    out = {"file": f"profiles/{name}.txt", "source": "committed ncu capture, not measured in this run",
+           "commit": prof.get("commit", "not recorded"), "command": prof.get("command")}
+    for k in ("fp64_pipe_active_pct", "issue_slots_used_pct", "dram_throughput_pct", "duration_us",
+              "traffic_bytes_per_launch", "traffic_scale"):
+        if k in prof:
+            out[k] = prof[k]
     return out
 
 
@@ -217,15 +266,10 @@ def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured
            "share_of_step_time": d["t"] * 1e3 / dev_ms if dev_ms > 0 else None,
            "peak_source": ("measured (MEASURED_PEAKS.json hbm_gbs), of measured" if measured
                            else "fallback 6.8 TB/s, of fallback"),
-           "whole_step_achieved": alg_step * steps / (dev_ms / 1e3) / 1e9}
-    if prof:
-        out["profile"] = f"profiles/{profile_name}.txt"
-        for k in ("fp64_pipe_active_pct", "issue_slots_used_pct", "dram_throughput_pct"):
-            if k in prof:
-                out[k + "_ncu"] = prof[k]
-        if precision == 64 and "fp64_pipe_active_pct" in prof:
-            out["note"] = ("FP64 gate arithmetic issues on the FP64 pipe (1/64 of the FP32 rate on this GPU); "
-                           "ncu's FP64-pipe activity for this kernel is the bound, not HBM")
+           "whole_step_achieved": alg_step * steps / (dev_ms / 1e3) / 1e9,
+           "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of the committed ncu capture "
+                             "(profile.commit), scaled to a full launch by traffic_scale"}
+    out["profile"] = profile_block(prof, profile_name)
     other = "stream" if dom == "pair" else "pair"
     o = kinds[other]
     out["other_kernel"] = {"kernel": o["kernel"], "achieved": o["bytes"] / o["t"] / 1e9 if o["t"] > 0 else 0.0,
@@ -401,6 +445,41 @@ def run_gpu(args):
     dev_ms_t = sum(a.elapsed_time(b) for a, b in evt)
     stt.close()
 
+    # the device-applied gates alone: the same circuit on a state that credits no gate the host
+    # resolved without touching the state
+    sd = engine.State(nq, precision=args.precision, stream=stream.cuda_stream,
+                      initial_buckets=1 << max(6, p["k"] - 4 + 1), device_updates_only=True)
+    sd.apply(gates)
+    sd.sync()
+    dev_upd_per_step = sd.stats()["amp_updates"]
+    sd.close()
+    fp64_fma_rate = engine.fp64_rate(local)
+
+    # the same circuit with FP32 amplitudes (FP64 norm and prune comparisons), timed the same way,
+    # and its fidelity against the FP64 result of the timed steps
+    fp32 = None
+    if args.precision == 64 and not args.no_fp32:
+        s32 = engine.State(nq, precision=32, stream=stream.cuda_stream, initial_buckets=1 << max(6, p["k"] - 4 + 1))
+        for _ in range(max(3, args.warmup)):
+            s32.set_zero()
+            s32.apply(gates)
+            s32.sync()
+        q0 = s32.stats()
+        ev32 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        timed_steps(s32, ev32)
+        s32.sync()
+        q1 = s32.stats()
+        ms32 = sum(a.elapsed_time(b) for a, b in ev32)
+        fid32, err32 = s32.compare(st)
+        fp32 = {"value": q0["amp_updates"] * args.steps / (ms32 / 1e3), "unit": "amp-updates/s",
+                "ms_per_step": ms32 / args.steps, "dtype": "f32",
+                "whole_step_achieved_gbs": q0["alg_bytes"] * args.steps / (ms32 / 1e3) / 1e9,
+                "whole_step_frac": q0["alg_bytes"] * args.steps / (ms32 / 1e3) / 1e9 / (
+                    (measured_peaks() or {}).get("hbm_gbs", 6800.0)),
+                "passes_per_step": (q1["passes"] - q0["passes"]) / args.steps, "fidelity_vs_fp64": fid32, "max_abs_err_vs_fp64": err32}
+        s32.close()
+
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -410,16 +489,29 @@ def run_gpu(args):
     roofline["pass_timing"] = ("per-pass CUDA events over the same number of further steps of the same circuit "
                                "(events between passes stop the launch overlap of the measured steps)")
     roofline["ms_per_step_with_pass_events"] = dev_ms_t / args.steps
+    prof = roofline.get("profile") or {}
+    roofline["fp64_pipe"] = {
+        "peak_fma_lane_ops_per_s": fp64_fma_rate,
+        "peak_source": "sqc_fp64_rate in this run: timed loop of independent DFMA chains, 8 blocks/SM",
+        "pipe_active_pct_ncu": prof.get("fp64_pipe_active_pct"),
+        "pipe_active_source": "committed ncu capture (roofline.profile), sm__pipe_fp64_cycles_active"}
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(gates, args.cpu_seconds, args.precision)
+        cpu["device_ratio_note"] = ("the oracle applies every gate, including those the engine resolves on the "
+                                    "host; device_amp_updates / cpu value is the ratio for device-applied work")
     out = {"metric": "amp-updates/s", "value": value, "unit": "amp-updates/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": f"f{args.precision}",
            "data": "synthetic", "config": config_dict(args.workload, p, args.precision, world),
            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": int(launches),
            "clocks": clk, "passes_per_step": passes_per_step, "gates_per_step": int(gates.size),
-           "wall_s_timed": t_wall}
+           "wall_s_timed": t_wall,
+           "device_amp_updates": {"value": dev_upd_per_step * args.steps * world / t_max, "unit": "amp-updates/s",
+                                  "per_step": dev_upd_per_step, "all_gates_per_step": upd_per_step,
+                                  "note": "gates applied on the device only; `value` also credits the gates the "
+                                          "host resolved without touching the state, as the reference runs them"},
+           "fp32": fp32}
     print(json.dumps(out), flush=True)
     st.close()
 

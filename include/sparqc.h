@@ -197,6 +197,30 @@ int sqc_measure(sqc_state* st, uint32_t qubit, double u, int* outcome, double* p
  * splitmix64 hash of (seed, s). The same state and seed give the same samples. */
 int sqc_sample(sqc_state* st, uint64_t shots, uint64_t seed, uint64_t* keys);
 
+/* ---- two-qubit gates ------------------------------------------------------------------ */
+/* No counterpart in the reference (its gates are eight uncontrolled single-qubit gates,
+ * emulator/include/circuit.h:45-83). A two-qubit gate on qubits (a, b) acts on the basis states
+ * indexed i_a + 2 i_b and is applied as a short sequence of this engine's own gates, which fuse
+ * into the usual passes:
+ *   SQC_2Q_UNITARY  any 4x4 unitary u (row-major (re, im) pairs, unitary to 1e-9): two-level
+ *                   rotations (controlled U and Phase gates) and a phase, at most 13 gates that
+ *                   act on amplitudes plus relabellings; results agree with the matrix to ~1e-15;
+ *   SQC_2Q_RZZ      exp(-i theta/2 Z_a Z_b), two controlled Rz;
+ *   SQC_2Q_ISWAP    [[1,0,0,0],[0,0,i,0],[0,i,0,0],[0,0,0,1]], exact (CNOTs and S);
+ *   SQC_2Q_FSIM     [[1,0,0,0],[0,cos t,-i sin t,0],[0,-i sin t,cos t,0],[0,0,0,e^{-i phi}]];
+ *   SQC_2Q_CSWAP    swap of a and b where qubit c is 1 (Fredkin), exact (three X gates);
+ *   SQC_2Q_SWAP     swap of a and b, exact.
+ * Every gate applies only where all `controls` bits are 1 (they may not include a, b or c). */
+enum { SQC_2Q_UNITARY = 0, SQC_2Q_RZZ = 1, SQC_2Q_ISWAP = 2, SQC_2Q_FSIM = 3, SQC_2Q_CSWAP = 4, SQC_2Q_SWAP = 5 };
+/* The gate sequence of one two-qubit gate (c: CSWAP's control qubit, else ignored; u: the
+ * matrix of SQC_2Q_UNITARY, else ignored) into out (capacity cap; 32 always suffice); *n
+ * receives the count. For batches, servers and partitioned states, which take gate arrays. */
+int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta, double phi,
+                   const double* u, sqc_gate* out, uint64_t cap, uint64_t* n);
+/* Apply one two-qubit gate to a state (the sequence of sqc_twoq_gates). */
+int sqc_apply_twoq(sqc_state* st, uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta,
+                   double phi, const double* u);
+
 /* Compare two states of equal qubit count on the device (FP64 accumulation):
  * fidelity = |<b|a>|^2 / (<a|a><b|b>), max_abs_err = max over keys of |a_k - b_k|. */
 int sqc_compare(sqc_state* a, sqc_state* b, double* fidelity, double* max_abs_err);
@@ -251,7 +275,10 @@ typedef struct sqc_batch_options {
     uint32_t blocks_per_sm;    /* persistent blocks per SM, 0 = as many as fit */
     uint64_t memory_budget;    /* bytes of device memory the batch may hold, 0 = 98% of the device */
     uint32_t use_graph;        /* 1: sqc_batch_run replays a captured CUDA graph */
-    uint32_t reserved[5];
+    uint32_t idle_limit_us;    /* a warp of the persistent kernel that finds no work for this long
+                                  ends the run, which then fails with SQC_ERR_STATE (every wait in
+                                  the kernel is bounded); 0 = 2 s */
+    uint32_t reserved[4];
 } sqc_batch_options;
 
 /* Tuning picked by sqc_batch_autotune. */
@@ -332,7 +359,11 @@ typedef struct sqc_server_options {
                                   single-state engine (pipelined large-table passes), a slice of
                                   their gates per step; 0 = default (17), 64 = never */
     uint32_t solo_share_pct;   /* percent of the budget kept for those circuits' tables, default 25 */
-    uint32_t reserved[4];
+    uint32_t inject_alloc_failures; /* testing aid for callers' error paths: the next N admissions
+                                  (a placement in the pool, or a large circuit's own tables) fail
+                                  as an out-of-memory device would: sqc_server_step returns
+                                  SQC_ERR_OOM and the request stays queued; 0 (default) = none */
+    uint32_t reserved[3];
 } sqc_server_options;
 
 enum { SQC_REQ_QUEUED = 0, SQC_REQ_RUNNING = 1, SQC_REQ_DONE = 2 };

@@ -81,6 +81,21 @@ public:
         for (uint32_t c : controls) m |= uint64_t(1) << c;
         gate(kind, t, theta, m, phi, lambda);
     }
+    /* two-qubit gates (sqc_apply_twoq); u: 4x4 row-major (re, im) pairs, index i_a + 2 i_b */
+    void unitary2(uint32_t a, uint32_t b, const double* u, uint64_t controls = 0) {
+        check(sqc_apply_twoq(st_, SQC_2Q_UNITARY, a, b, 0, controls, 0.0, 0.0, u), "unitary2");
+    }
+    void rzz(uint32_t a, uint32_t b, double theta) {
+        check(sqc_apply_twoq(st_, SQC_2Q_RZZ, a, b, 0, 0, theta, 0.0, nullptr), "rzz");
+    }
+    void iswap(uint32_t a, uint32_t b) { check(sqc_apply_twoq(st_, SQC_2Q_ISWAP, a, b, 0, 0, 0.0, 0.0, nullptr), "iswap"); }
+    void fsim(uint32_t a, uint32_t b, double theta, double phi) {
+        check(sqc_apply_twoq(st_, SQC_2Q_FSIM, a, b, 0, 0, theta, phi, nullptr), "fsim");
+    }
+    void cswap(uint32_t c, uint32_t a, uint32_t b) {
+        check(sqc_apply_twoq(st_, SQC_2Q_CSWAP, a, b, c, 0, 0.0, 0.0, nullptr), "cswap");
+    }
+    void swap(uint32_t a, uint32_t b) { check(sqc_apply_twoq(st_, SQC_2Q_SWAP, a, b, 0, 0, 0.0, 0.0, nullptr), "swap"); }
     void apply(const std::vector<sqc_gate>& gates) {
         check(sqc_apply_gates(st_, gates.data(), gates.size()), "apply");
     }

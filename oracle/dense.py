@@ -34,6 +34,21 @@ def matrix(kind, theta=0.0, phi=0.0, lam=0.0):
     return np.asarray(m, dtype=np.complex128)
 
 
+def matrix2(form, theta=0.0, phi=0.0):
+    """Textbook 4x4 matrices of the named two-qubit gates over the index i_a + 2 i_b (CSWAP: the
+    SWAP it applies where its control is 1). Forms numbered as the engine's SQC_2Q_*."""
+    c, s = np.cos(theta), np.sin(theta)
+    e = np.exp(-0.5j * theta)
+    m = {
+        1: np.diag([e, np.conj(e), np.conj(e), e]),                                  # RZZ
+        2: [[1, 0, 0, 0], [0, 0, 1j, 0], [0, 1j, 0, 0], [0, 0, 0, 1]],                # iSWAP
+        3: [[1, 0, 0, 0], [0, c, -1j * s, 0], [0, -1j * s, c, 0], [0, 0, 0, np.exp(-1j * phi)]],   # fSim
+        4: [[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]],                  # CSWAP's SWAP
+        5: [[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]],                  # SWAP
+    }[form]
+    return np.asarray(m, dtype=np.complex128)
+
+
 class DenseOracle:
     def __init__(self, nq):
         if nq > 26:
@@ -63,6 +78,17 @@ class DenseOracle:
         a1 = self.psi[i1].copy()
         self.psi[i0] = m[0, 0] * a0 + m[0, 1] * a1
         self.psi[i1] = m[1, 0] * a0 + m[1, 1] * a1
+
+    def apply_matrix2(self, a, b, controls, m):
+        """A 4x4 matrix m on qubits (a, b), index i_a + 2 i_b, where every control bit is 1."""
+        ba, bb = np.uint64(1 << a), np.uint64(1 << b)
+        idx = self._idx
+        sel = ((idx & (ba | bb)) == 0) & ((idx & np.uint64(controls)) == np.uint64(controls))
+        i0 = idx[sel].astype(np.int64)
+        grp = [i0, i0 | (1 << a), i0 | (1 << b), i0 | (1 << a) | (1 << b)]
+        v = [self.psi[g].copy() for g in grp]
+        for r in range(4):
+            self.psi[grp[r]] = sum(m[r, k] * v[k] for k in range(4))
 
     def state(self, threshold=1e-14):
         """Key-sorted entries whose amplitude is not negligible (|re|,|im| < threshold)."""

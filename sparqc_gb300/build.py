@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsparqc.so")
 SOURCES = ["sqc_pass.cu", "sqc_kernels.cu", "sqc_batch.cu", "sqc_measure.cu", "sqc_engine.cpp", "sqc_plan.cpp", "sqc_batch.cpp",
            "sqc_serve.cpp",
-           "sqc_capi.cpp", "sqc_capi_batch.cpp", "sqc_fixed.cu", "sqc_part.cpp", "sqc_capi_part.cpp"]
+           "sqc_capi.cpp", "sqc_capi_batch.cpp", "sqc_fixed.cu", "sqc_part.cpp", "sqc_capi_part.cpp", "sqc_twoq.cpp"]
 # per-file extra flags: the persistent batch kernel reads data other SMs wrote during the
 # same launch, so its global loads default to L2 (L1 is not coherent across SMs)
 EXTRA = {"sqc_batch.cu": ["-Xptxas", "-dlcm=cg"]}

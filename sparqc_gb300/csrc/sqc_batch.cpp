@@ -128,6 +128,7 @@ int Batch::init(const sqc_batch_options* opt) {
     lf_ = o.load_factor;
     min_chunk_ = o.min_chunk;
     blocks_per_sm_ = o.blocks_per_sm;
+    idle_limit_ns_ = o.idle_limit_us ? 1000ULL * o.idle_limit_us : 2000000000ULL;
     use_graph_ = o.use_graph != 0;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
@@ -297,6 +298,7 @@ BatchArgs Batch::args() const {
     const unsigned long long warps = (unsigned long long)grid() * 8;
     a.target_chunks = (uint32_t)std::min<unsigned long long>(kMaxChunks, std::max<unsigned long long>(4 * warps, 1));
     a.prune = prune_;
+    a.idle_limit_ns = idle_limit_ns_;
     return a;
 }
 

@@ -14,8 +14,9 @@
 // Gate descriptors and the circuit array never change during a launch and are read through
 // the read-only path (plain non-coherent loads, without the pass kernels' L1 priority hint).
 //
-// A warp that finds no work sleeps briefly and retries; after kIdleLimitNs without work it
-// records ST_TIMEOUT in the batch control block and returns. Parking: when the batch has a
+// A warp that finds no work sleeps briefly and retries; after idle_limit_ns without work it
+// records ST_TIMEOUT in the batch control block and returns (the limit is a batch option,
+// 2 s by default); every warp returns at its next check of that status. Parking: when the batch has a
 // deadline, a circuit whose pass ends after the deadline parks instead of opening its next
 // pass; a later launch resumes it (used by the serving loop to admit new circuits).
 #define SQC_DESC_EVICT_LAST 0
@@ -30,7 +31,6 @@ constexpr int kBatchThreads = 256;
 // 256-circuit batch); FP64 circuits read them in place (their registers are tighter: the copy
 // cost 4%).
 template <class T> struct BatchStage { static constexpr bool kOn = sizeof(T) == 4; };
-constexpr unsigned long long kIdleLimitNs = 2000000000ULL;   // 2 s without work: give up
 constexpr unsigned kIdleSleepNs = 1000;                       // back-off of a warp that found no work
 
 __device__ __forceinline__ unsigned long long sched_word(unsigned long long pass, unsigned long long chunks) {
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kBatchThreads, MINB) batch_run_kernel(BatchArg
             if (lane == 0) {
                 const unsigned long long now = globaltimer();
                 if (!idle_since) idle_since = now;
-                else if (now - idle_since > kIdleLimitNs) atomicCAS(&a.bctl->status, 0u, (unsigned)ST_TIMEOUT);
+                else if (now - idle_since > a.idle_limit_ns) atomicCAS(&a.bctl->status, 0u, (unsigned)ST_TIMEOUT);
             }
             __syncwarp();
             __nanosleep(kIdleSleepNs);

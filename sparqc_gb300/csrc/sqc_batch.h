@@ -91,6 +91,7 @@ private:
     PruneBits prune_{};
     double lf_ = 0.45;
     uint32_t min_chunk_ = 8;
+    unsigned long long idle_limit_ns_ = 2000000000ULL;   // a warp without work for this long ends the run
     uint32_t blocks_per_sm_ = 0;   // 0: occupancy
     bool use_graph_ = false;
     size_t budget_ = 0;

@@ -77,6 +77,7 @@ struct BatchArgs {
     uint32_t min_chunk;             // list entries per chunk at least (a multiple of 4)
     uint32_t target_chunks;         // chunks per pass at most, for large circuits
     PruneBits prune;
+    unsigned long long idle_limit_ns;   // a warp that finds no work for this long records ST_TIMEOUT
 };
 
 }  // namespace sqc

@@ -3,10 +3,12 @@
 // CUDA errors, emulator/device/table_manager.cuh:175-259, emulator/third_party/helper_cuda.h).
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/sparqc.h"
 #include "sqc_handles.h"
 #include "sqc_kernels.h"
+#include "sqc_twoq.h"
 
 namespace {
 
@@ -170,6 +172,33 @@ int sqc_sample(sqc_state* st, uint64_t shots, uint64_t seed, uint64_t* keys) {
 int sqc_get_stats(sqc_state* st, sqc_stats* out) {
     if (!out) return SQC_ERR_ARG;
     return guarded(st, [&](sqc::Engine& e) { return e.stats(out); });
+}
+
+int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta, double phi,
+                   const double* u, sqc_gate* out, uint64_t cap, uint64_t* n) {
+    if (!n) return SQC_ERR_ARG;
+    *n = 0;
+    std::vector<sqc_gate> g;
+    const int rc = sqc::twoq_sequence(form, a, b, c, controls, theta, phi, u, g);
+    if (rc) return rc;
+    *n = g.size();
+    if (g.size() > cap) return SQC_ERR_CAPACITY;
+    if (!g.empty() && !out) return SQC_ERR_ARG;
+    for (size_t i = 0; i < g.size(); ++i) out[i] = g[i];
+    return SQC_OK;
+}
+
+int sqc_apply_twoq(sqc_state* st, uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta,
+                   double phi, const double* u) {
+    return guarded(st, [&](sqc::Engine& e) {
+        std::vector<sqc_gate> g;
+        const int rc = sqc::twoq_sequence(form, a, b, c, controls, theta, phi, u, g);
+        if (rc) {
+            e.err = "bad two-qubit gate (qubits, controls, form or matrix)";
+            return rc;
+        }
+        return e.apply(g.data(), g.size());
+    });
 }
 
 int sqc_fp64_rate(uint32_t device, double* fma_per_s) {

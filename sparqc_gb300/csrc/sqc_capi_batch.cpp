@@ -48,7 +48,8 @@ void sqc_batch_default_options(sqc_batch_options* opt) {
     opt->blocks_per_sm = 0;
     opt->memory_budget = 0;
     opt->use_graph = 0;
-    for (int i = 0; i < 5; ++i) opt->reserved[i] = 0;
+    opt->idle_limit_us = 0;
+    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_batch_create(const sqc_batch_options* opt, sqc_batch** out) {
@@ -147,7 +148,8 @@ void sqc_server_default_options(sqc_server_options* opt) {
     opt->slice_ms = 2.0;
     opt->solo_log2_groups = 0;
     opt->solo_share_pct = 25;
-    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
+    opt->inject_alloc_failures = 0;
+    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_server_create(const sqc_server_options* opt, sqc_server** out) {

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "sqc_exact.cuh"
 #include "sqc_kernels.h"
 
 namespace sqc {
@@ -34,6 +35,8 @@ Engine::~Engine() {
     free_table(&tab_);
     if (ctl_) cudaFree(ctl_);
     if (ctl_host_) cudaFreeHost(ctl_host_);
+    if (sums_) cudaFree(sums_);
+    if (sums_host_) cudaFreeHost(sums_host_);
     if (d_desc_) cudaFree(d_desc_);
     if (h_desc_) cudaFreeHost(h_desc_);
     if (d_tiny_) cudaFree(d_tiny_);
@@ -125,6 +128,8 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     if ((rc = cuda(cudaMalloc(&ctl_, sizeof(Ctl)), "cudaMalloc(ctl)"))) return rc;
     if ((rc = cuda(cudaMemset(ctl_, 0, sizeof(Ctl)), "cudaMemset(ctl)"))) return rc;
     if ((rc = cuda(cudaMallocHost(&ctl_host_, sizeof(Ctl)), "cudaMallocHost(ctl)"))) return rc;
+    if ((rc = cuda(cudaMalloc(&sums_, sizeof(ExactSums)), "cudaMalloc(sums)"))) return rc;
+    if ((rc = cuda(cudaMallocHost(&sums_host_, sizeof(ExactSums)), "cudaMallocHost(sums)"))) return rc;
     std::memset(ctl_host_, 0, sizeof(Ctl));
     if ((rc = ensure_desc(kDescInitial))) return rc;
 
@@ -459,6 +464,55 @@ int Engine::flush(bool hold_last) {
     return SQC_OK;
 }
 
+int Engine::read_sums() {
+    int rc;
+    if ((rc = cuda(cudaMemcpyAsync(sums_host_, sums_, sizeof(ExactSums), cudaMemcpyDeviceToHost, stream_), "D2H sums")))
+        return rc;
+    return cuda(cudaStreamSynchronize(stream_), "sync");
+}
+
+// The exact total of a fixed-point accumulator (sqc_exact.cuh), rounded to the nearest double.
+double exact_sum_value(const unsigned long long* acc) {
+    uint32_t limb[kSumChunks];
+    unsigned __int128 carry = 0;
+    for (int i = 0; i < kSumChunks; ++i) {   // carry the pieces into 32-bit limbs (mod 2^(32 kSumChunks))
+        const unsigned __int128 v = (unsigned __int128)acc[i] + carry;
+        limb[i] = (uint32_t)v;
+        carry = v >> 32;
+    }
+    const bool neg = (limb[kSumChunks - 1] >> 31) != 0;   // two's complement sign
+    if (neg) {
+        uint64_t c = 1;
+        for (int i = 0; i < kSumChunks; ++i) {
+            const uint64_t v = (uint64_t)(uint32_t)~limb[i] + c;
+            limb[i] = (uint32_t)v;
+            c = v >> 32;
+        }
+    }
+    int h = kSumChunks - 1;
+    while (h >= 0 && !limb[h]) --h;
+    if (h < 0) return 0.0;
+    // the top three limbs, the rest as a sticky bit; round to 53 bits, ties to even
+    unsigned __int128 w = ((unsigned __int128)limb[h] << 64) | ((unsigned __int128)(h >= 1 ? limb[h - 1] : 0u) << 32) |
+                          (unsigned __int128)(h >= 2 ? limb[h - 2] : 0u);
+    bool sticky = false;
+    for (int i = 0; i < h - 2; ++i) sticky = sticky || limb[i] != 0;
+    int scale = 32 * (h - 2) + kSumLsb;   // weight of w's least significant bit
+    int bits = 0;
+    for (unsigned __int128 t = w; t; t >>= 1) ++bits;
+    uint64_t m = (uint64_t)w;
+    if (bits > 53) {
+        const int drop = bits - 53;
+        const unsigned __int128 rem = w & (((unsigned __int128)1 << drop) - 1);
+        const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
+        m = (uint64_t)(w >> drop);
+        if (rem > half || (rem == half && (sticky || (m & 1)))) ++m;
+        scale += drop;
+    }
+    const double v = std::ldexp((double)m, scale);
+    return neg ? -v : v;
+}
+
 int Engine::read_ctl() {
     int rc;
     if ((rc = cuda(cudaMemcpyAsync(ctl_host_, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_), "D2H ctl")))
@@ -774,14 +828,14 @@ int Engine::probability(uint64_t mask, uint64_t value, double* p) {
     if (!p) return fail(SQC_ERR_ARG, "null output");
     int rc = sync();
     if (rc) return rc;
-    if ((rc = cuda(cudaMemsetAsync(&ctl_->acc[0], 0, sizeof(double), stream_), "memset")) ||
-        (rc = cuda(launch_pattern_prob(dev(), ctl_, list_hint_, dbl_, mask, value ^ (plan_.frame & mask), sms_,
+    if ((rc = cuda(cudaMemsetAsync(sums_, 0, sizeof(ExactSums), stream_), "memset")) ||
+        (rc = cuda(launch_pattern_prob(dev(), ctl_, list_hint_, dbl_, mask, value ^ (plan_.frame & mask), sums_, sms_,
                                        stream_),
                    "probability")))
         return rc;
     ++launches_;
-    if ((rc = read_ctl())) return rc;
-    *p = ctl_host_->acc[0];
+    if ((rc = read_sums())) return rc;
+    *p = exact_sum_value(sums_host_->c[SUM_NORM]);
     return SQC_OK;
 }
 
@@ -839,11 +893,11 @@ int Engine::sample(uint64_t shots, uint64_t seed, uint64_t* keys) {
 int Engine::norm2(double* out) {
     int rc = sync();
     if (rc) return rc;
-    if ((rc = cuda(cudaMemsetAsync(&ctl_->acc[0], 0, sizeof(double), stream_), "memset"))) return rc;
-    if ((rc = cuda(launch_norm(dev(), ctl_, list_hint_, dbl_, sms_, stream_), "norm"))) return rc;
+    if ((rc = cuda(cudaMemsetAsync(sums_, 0, sizeof(ExactSums), stream_), "memset"))) return rc;
+    if ((rc = cuda(launch_norm(dev(), ctl_, list_hint_, dbl_, sums_, sms_, stream_), "norm"))) return rc;
     ++launches_;
-    if ((rc = read_ctl())) return rc;
-    *out = ctl_host_->acc[0];
+    if ((rc = read_sums())) return rc;
+    *out = exact_sum_value(sums_host_->c[SUM_NORM]);
     return SQC_OK;
 }
 
@@ -861,17 +915,22 @@ int Engine::compare_with(const TableDev& tb, const Ctl* cb, unsigned long long h
     if (device_b != device_) return fail(SQC_ERR_ARG, "states live on different devices");
     int rc;
     if ((rc = sync())) return rc;
-    if ((rc = cuda(cudaMemsetAsync(ctl_->acc, 0, sizeof(ctl_->acc), stream_), "memset")) ||
+    if ((rc = cuda(cudaMemsetAsync(sums_, 0, sizeof(ExactSums), stream_), "memset")) ||
         (rc = cuda(cudaMemsetAsync(&ctl_->acc_max, 0, sizeof(unsigned long long), stream_), "memset")))
         return rc;
     if ((rc = cuda(launch_compare(dev(), ctl_, list_hint_, dbl_, tb, cb, std::max<unsigned long long>(hint_b, 1),
-                                  dbl_b, plan_.frame ^ frame_b, ctl_, sms_, stream_),
+                                  dbl_b, plan_.frame ^ frame_b, ctl_, sums_, sms_, stream_),
                    "compare")))
         return rc;
-    launches_ += 2;
+    launches_ += 3;
+    if ((rc = read_sums())) return rc;
     if ((rc = read_ctl())) return rc;
-    const double ore = ctl_host_->acc[0], oim = ctl_host_->acc[1], na = ctl_host_->acc[2];
-    const double nb = ctl_host_->acc[3] + ctl_host_->acc[4];
+    const double ore = exact_sum_value(sums_host_->c[SUM_ORE]), oim = exact_sum_value(sums_host_->c[SUM_OIM]);
+    const double na = exact_sum_value(sums_host_->c[SUM_NA]);
+    // |b|^2 over b's keys: those a shares and those it lacks, added exactly before rounding
+    unsigned long long nbc[kSumChunks];
+    for (int i = 0; i < kSumChunks; ++i) nbc[i] = sums_host_->c[SUM_NB][i] + sums_host_->c[SUM_NB_ONLY][i];
+    const double nb = exact_sum_value(nbc);
     double mx;
     std::memcpy(&mx, &ctl_host_->acc_max, sizeof(double));
     *fidelity = (na > 0 && nb > 0) ? (ore * ore + oim * oim) / (na * nb) : 0.0;

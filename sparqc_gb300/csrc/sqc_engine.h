@@ -100,6 +100,7 @@ private:
     int readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got);
     bool plan_gate(const sqc_gate& g, GateDesc* out);
     int read_ctl();
+    int read_sums();   // copy the exact sums back and wait
     int record_event(cudaEvent_t* out);
     void harvest_events();
     unsigned long long max_groups() const;
@@ -120,6 +121,8 @@ private:
     HostTable tab_;
     Ctl* ctl_ = nullptr;        // device
     Ctl* ctl_host_ = nullptr;   // pinned mirror
+    ExactSums* sums_ = nullptr;       // device: exact sums of norm, probability and compare
+    ExactSums* sums_host_ = nullptr;  // pinned mirror
     unsigned long long seq_verified_ = 0;
     unsigned long long list_hint_ = 1;
     PruneBits prune_{};

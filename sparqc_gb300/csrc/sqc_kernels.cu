@@ -2,6 +2,7 @@
 // counting, readout, norm, state comparison and table rebuild. All walk the list of live
 // buckets. The gate passes are in sqc_pass.cu.
 #include "sqc_kernels.h"
+#include "sqc_exact.cuh"
 
 #include <algorithm>
 
@@ -224,21 +225,21 @@ __global__ void readout_kernel(TableDev t, Ctl* ctl, unsigned long long frame, u
     }
 }
 
-// Sum of |a|^2 over the state, accumulated in FP64, into ctl->acc[0].
+// Sum of |a|^2 over the state, exactly (sqc_exact.cuh), into sums->c[SUM_NORM].
 template <class T>
-__global__ void norm_kernel(TableDev t, Ctl* ctl) {
+__global__ void norm_kernel(TableDev t, Ctl* ctl, ExactSums* sums) {
     const unsigned long long n = ctl->list_n;
-    double acc = 0.0;
+    unsigned long long acc[kSumChunks] = {};
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
         const size_t slot = (size_t)t.list[s >> kSlotBits] * kSlots + (s & 15);
         if (!slot_present(t.keys[slot], (int)(s & 15))) continue;
         const Cx<T> v = load_amp<T>(t.amps, slot);
         const double r = (double)v.r, i = (double)v.i;
-        acc = __fma_rn(r, r, __fma_rn(i, i, acc));
+        exact_add_prod(acc, r, r);
+        exact_add_prod(acc, i, i);
     }
-    acc = warp_sum(acc);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&ctl->acc[0], acc);
+    exact_flush(acc, sums->c[SUM_NORM]);
 }
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double v) {
@@ -257,13 +258,17 @@ __device__ __forceinline__ bool find_other(const TableDev& tb, unsigned ep_b, un
     return true;
 }
 
-// Over the keys of a: acc[0..1] += conj(b)*a, acc[2] += |a|^2, acc[3] += |b|^2, max |a-b|.
-// d = frame_a ^ frame_b translates a stored key of a into b's frame.
+// Over the keys of a, exactly (sqc_exact.cuh): PART 0 sums conj(b)*a (real part into
+// SUM_ORE, imaginary into SUM_OIM), PART 1 sums |a|^2 (SUM_NA) and |b|^2 (SUM_NB) and takes the
+// max |a-b| (a max does not depend on the order). Two accumulators per launch keep the
+// registers in check. d = frame_a ^ frame_b translates a stored key of a into b's frame.
+template <int PART>
 __global__ void compare_a_kernel(TableDev ta, const Ctl* ca, int dbl_a, TableDev tb, const Ctl* cb, int dbl_b,
-                                 unsigned long long d, Ctl* out) {
+                                 unsigned long long d, Ctl* out, ExactSums* sums) {
     const unsigned long long n = ca->list_n;
     const unsigned ep_b = cb->epoch;
-    double ore = 0, oim = 0, na = 0, nbb = 0, mx = 0;
+    unsigned long long s0[kSumChunks] = {}, s1[kSumChunks] = {};
+    double mx = 0;
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
         const size_t slot = (size_t)ta.list[s >> kSlotBits] * kSlots + (s & 15);
@@ -272,30 +277,35 @@ __global__ void compare_a_kernel(TableDev ta, const Ctl* ca, int dbl_a, TableDev
         const Cx<double> va = load_amp_any(ta.amps, slot, dbl_a);
         Cx<double> vb{0.0, 0.0};
         find_other(tb, ep_b, key ^ d, dbl_b, &vb);
-        ore += vb.r * va.r + vb.i * va.i;
-        oim += vb.r * va.i - vb.i * va.r;
-        na += va.r * va.r + va.i * va.i;
-        nbb += vb.r * vb.r + vb.i * vb.i;
-        const double dr = va.r - vb.r, di = va.i - vb.i;
-        mx = fmax(mx, sqrt(dr * dr + di * di));
+        if (PART == 0) {
+            exact_add_prod(s0, vb.r, va.r);
+            exact_add_prod(s0, vb.i, va.i);
+            exact_add_prod(s1, vb.r, va.i);
+            exact_add_prod(s1, -vb.i, va.r);
+        } else {
+            exact_add_prod(s0, va.r, va.r);
+            exact_add_prod(s0, va.i, va.i);
+            exact_add_prod(s1, vb.r, vb.r);
+            exact_add_prod(s1, vb.i, vb.i);
+            const double dr = va.r - vb.r, di = va.i - vb.i;
+            mx = fmax(mx, sqrt(dr * dr + di * di));
+        }
     }
-    ore = warp_sum(ore); oim = warp_sum(oim); na = warp_sum(na); nbb = warp_sum(nbb);
-    for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(kFull, mx, o));
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&out->acc[0], ore);
-        atomicAdd(&out->acc[1], oim);
-        atomicAdd(&out->acc[2], na);
-        atomicAdd(&out->acc[3], nbb);
-        atomic_max_nonneg(&out->acc_max, mx);
+    exact_flush(s0, sums->c[PART == 0 ? SUM_ORE : SUM_NA]);
+    exact_flush(s1, sums->c[PART == 0 ? SUM_OIM : SUM_NB]);
+    if (PART == 1) {
+        for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(kFull, mx, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&out->acc_max, mx);
     }
 }
 
-// Keys of b absent from a: acc[4] += |b|^2, max |b|.
+// Keys of b absent from a: SUM_NB_ONLY += |b|^2 (exactly), max |b|.
 __global__ void compare_b_kernel(TableDev ta, const Ctl* ca, TableDev tb, const Ctl* cb, int dbl_b,
-                                 unsigned long long d, Ctl* out) {
+                                 unsigned long long d, Ctl* out, ExactSums* sums) {
     const unsigned long long n = cb->list_n;
     const unsigned ep_a = ca->epoch;
-    double nbo = 0, mx = 0;
+    unsigned long long s0[kSumChunks] = {};
+    double mx = 0;
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
         const size_t slot = (size_t)tb.list[s >> kSlotBits] * kSlots + (s & 15);
@@ -304,15 +314,13 @@ __global__ void compare_b_kernel(TableDev ta, const Ctl* ca, TableDev tb, const 
         Cx<double> dummy;
         if (find_other(ta, ep_a, key ^ d, true, &dummy)) continue;
         const Cx<double> vb = load_amp_any(tb.amps, slot, dbl_b);
-        nbo += vb.r * vb.r + vb.i * vb.i;
+        exact_add_prod(s0, vb.r, vb.r);
+        exact_add_prod(s0, vb.i, vb.i);
         mx = fmax(mx, sqrt(vb.r * vb.r + vb.i * vb.i));
     }
-    nbo = warp_sum(nbo);
+    exact_flush(s0, sums->c[SUM_NB_ONLY]);
     for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_down_sync(kFull, mx, o));
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&out->acc[4], nbo);
-        atomic_max_nonneg(&out->acc_max, mx);
-    }
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&out->acc_max, mx);
 }
 
 // Copy the live, non-empty buckets of the old table into a new one (fresh headers, epoch
@@ -403,18 +411,22 @@ cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_
     return cudaGetLastError();
 }
 
-cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st) {
+cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, ExactSums* sums, int sms,
+                        cudaStream_t st) {
     const int grid = grid_for(list_hint * kSlots + 1, kThreads, sms);
-    if (dbl) norm_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl);
-    else norm_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl);
+    if (dbl) norm_kernel<double><<<grid, kThreads, 0, st>>>(t, ctl, sums);
+    else norm_kernel<float><<<grid, kThreads, 0, st>>>(t, ctl, sums);
     return cudaGetLastError();
 }
 
 cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,
                            const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
-                           unsigned long long d, Ctl* out, int sms, cudaStream_t st) {
-    compare_a_kernel<<<grid_for(hint_a * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(ta, ca, dbl_a, tb, cb, dbl_b, d, out);
-    compare_b_kernel<<<grid_for(hint_b * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(ta, ca, tb, cb, dbl_b, d, out);
+                           unsigned long long d, Ctl* out, ExactSums* sums, int sms, cudaStream_t st) {
+    const int ga = grid_for(hint_a * kSlots + 1, kThreads, sms);
+    compare_a_kernel<0><<<ga, kThreads, 0, st>>>(ta, ca, dbl_a, tb, cb, dbl_b, d, out, sums);
+    compare_a_kernel<1><<<ga, kThreads, 0, st>>>(ta, ca, dbl_a, tb, cb, dbl_b, d, out, sums);
+    compare_b_kernel<<<grid_for(hint_b * kSlots + 1, kThreads, sms), kThreads, 0, st>>>(ta, ca, tb, cb, dbl_b, d, out,
+                                                                                        sums);
     return cudaGetLastError();
 }
 

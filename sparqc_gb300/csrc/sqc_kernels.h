@@ -28,11 +28,12 @@ cudaError_t launch_readout(const TableDev& t, Ctl* ctl, unsigned long long list_
                            bool dbl, unsigned long long* okeys, double* ore, double* oim, unsigned long long cap,
                            bool drop_negl, PruneBits pb, int sms, cudaStream_t st, unsigned long long smask = 0,
                            unsigned long long sval = 0);
-cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, int sms,
+// Exact sum of |a|^2 into sums->c[SUM_NORM] (sqc_exact.cuh); the caller zeroes it first.
+cudaError_t launch_norm(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl, ExactSums* sums, int sms,
                         cudaStream_t st);
 cudaError_t launch_compare(const TableDev& ta, const Ctl* ca, unsigned long long hint_a, bool dbl_a,
                            const TableDev& tb, const Ctl* cb, unsigned long long hint_b, bool dbl_b,
-                           unsigned long long d, Ctl* out, int sms, cudaStream_t st);
+                           unsigned long long d, Ctl* out, ExactSums* sums, int sms, cudaStream_t st);
 // Measured FP64 fused multiply-add rate of the current device (lane operations per second), from
 // a timed loop of independent FMA chains over sms * 8 blocks. Synchronizes the device.
 cudaError_t measure_fp64_rate(int sms, double* fma_per_s);

@@ -8,12 +8,13 @@
 //
 // Keys in the table are stored in the planner's frame (stored = actual ^ frame); a pattern on
 // actual keys (actual & mask) == value is tested as (stored & mask) == (value ^ (frame & mask)).
-// Probability sums accumulate in FP64 with atomics, so their last bits depend on the order the
-// warps finish in; gate application never reads them.
+// Probability sums are exact (sqc_exact.cuh) and rounded once, so they do not depend on the
+// order in which the warps meet the keys; a measurement outcome is reproducible.
 #include <algorithm>
 
 #include <cub/cub.cuh>
 
+#include "sqc_exact.cuh"
 #include "sqc_kernels.h"
 #include "sqc_measure.h"
 
@@ -36,11 +37,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-// acc[0] += sum of |a|^2 over present keys with (stored & smask) == sval.
+// sums->c[SUM_NORM] += sum of |a|^2 over present keys with (stored & smask) == sval, exactly.
 template <class T>
-__global__ void pattern_prob_kernel(TableDev t, Ctl* ctl, unsigned long long smask, unsigned long long sval) {
+__global__ void pattern_prob_kernel(TableDev t, Ctl* ctl, unsigned long long smask, unsigned long long sval,
+                                    ExactSums* sums) {
     const unsigned long long n = ctl->list_n;
-    double acc = 0.0;
+    unsigned long long acc[kSumChunks] = {};
     for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < n * kSlots;
          s += (unsigned long long)gridDim.x * blockDim.x) {
         const size_t slot = (size_t)t.list[s >> kSlotBits] * kSlots + (s & 15);
@@ -48,10 +50,10 @@ __global__ void pattern_prob_kernel(TableDev t, Ctl* ctl, unsigned long long sma
         if (!((int)(key & 15ULL) == (int)(s & 15)) || (key & smask) != sval) continue;
         const Cx<T> v = amp_at<T>(t.amps, slot);
         const double r = (double)v.r, i = (double)v.i;
-        acc = __fma_rn(r, r, __fma_rn(i, i, acc));
+        exact_add_prod(acc, r, r);
+        exact_add_prod(acc, i, i);
     }
-    acc = warp_sum_d(acc);
-    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&ctl->acc[0], acc);
+    exact_flush(acc, sums->c[SUM_NORM]);
 }
 
 // Projective collapse: present keys with (stored & smask) != sval are removed, the others
@@ -141,10 +143,11 @@ int grid_of(unsigned long long items, int sms) {
 }  // namespace
 
 cudaError_t launch_pattern_prob(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl,
-                                unsigned long long smask, unsigned long long sval, int sms, cudaStream_t st) {
+                                unsigned long long smask, unsigned long long sval, ExactSums* sums, int sms,
+                                cudaStream_t st) {
     const int g = grid_of(list_hint * kSlots + 1, sms);
-    if (dbl) pattern_prob_kernel<double><<<g, 256, 0, st>>>(t, ctl, smask, sval);
-    else pattern_prob_kernel<float><<<g, 256, 0, st>>>(t, ctl, smask, sval);
+    if (dbl) pattern_prob_kernel<double><<<g, 256, 0, st>>>(t, ctl, smask, sval, sums);
+    else pattern_prob_kernel<float><<<g, 256, 0, st>>>(t, ctl, smask, sval, sums);
     return cudaGetLastError();
 }
 

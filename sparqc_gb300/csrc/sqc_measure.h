@@ -24,9 +24,11 @@ struct SortBuffers {
     size_t tmp_bytes = 0;
 };
 
-// acc[0] += sum of |a|^2 over present stored keys with (key & smask) == sval.
+// sums->c[SUM_NORM] += sum of |a|^2 over present stored keys with (key & smask) == sval
+// (exact; the caller zeroes it first).
 cudaError_t launch_pattern_prob(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl,
-                                unsigned long long smask, unsigned long long sval, int sms, cudaStream_t st);
+                                unsigned long long smask, unsigned long long sval, ExactSums* sums, int sms,
+                                cudaStream_t st);
 // Remove present keys with (key & smask) != sval, scale the others by `scale`, set nnz.
 cudaError_t launch_collapse(const TableDev& t, Ctl* ctl, unsigned long long list_hint, bool dbl,
                             unsigned long long smask, unsigned long long sval, double scale, int sms, cudaStream_t st);

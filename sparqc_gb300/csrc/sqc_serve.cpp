@@ -63,6 +63,7 @@ int Server::init(const sqc_server_options* opt) {
     min_chunk_ = o.min_chunk;
     max_slots_ = o.max_slots;
     slice_ms_ = o.slice_ms;
+    inject_fail_ = o.inject_alloc_failures;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
     float tf = (float)o.prune_threshold;
@@ -149,6 +150,10 @@ size_t Server::solo_bytes(const Request& r) const {
 }
 
 int Server::admit_solo(uint64_t rid, Request& r) {
+    if (inject_fail_) {   // testing aid: fail as an out-of-memory device would; nothing is held
+        --inject_fail_;
+        return fail(SQC_ERR_OOM, "injected allocation failure (large circuit's tables)");
+    }
     sqc_options o;
     sqc_default_options(&o);
     o.precision = dbl_ ? SQC_FP64 : SQC_FP32;
@@ -187,6 +192,10 @@ int Server::admit() {
             continue;
         }
         if (free_slots_.empty()) break;
+        if (inject_fail_) {   // testing aid: fail as an out-of-memory device would; the request stays queued
+            --inject_fail_;
+            return fail(SQC_ERR_OOM, "injected allocation failure (pool placement)");
+        }
         const size_t bytes = request_bytes(r);
         const size_t off = alloc_.alloc(bytes);
         if (off == SIZE_MAX) break;
@@ -244,6 +253,7 @@ BatchArgs Server::args(uint32_t n) const {
     const unsigned long long warps = (unsigned long long)sms_ * batch_residency(dbl_, 0) * 8;
     a.target_chunks = (uint32_t)std::min<unsigned long long>(kMaxChunks, 4 * warps);
     a.prune = prune_;
+    a.idle_limit_ns = 2000000000ULL;   // a warp without work for 2 s ends the slice with ST_TIMEOUT
     return a;
 }
 

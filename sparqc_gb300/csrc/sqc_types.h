@@ -108,6 +108,15 @@ struct PruneBits {
 
 constexpr uint32_t kNoQubit = 0xFFFFFFFFu;
 
+// Exact sums of products (sqc_exact.cuh): fixed-point numbers with their least significant bit
+// at 2^kSumLsb, kSumChunks 32-bit pieces each held in a 64-bit counter.
+constexpr int kSumChunks = 10;
+constexpr int kSumLsb = -256;
+enum SumIndex { SUM_NORM = 0, SUM_ORE, SUM_OIM, SUM_NA, SUM_NB, SUM_NB_ONLY, kSums };
+struct ExactSums {
+    unsigned long long c[kSums][kSumChunks];
+};
+
 // One pass of a single-launch run over a tiny table (tiny_kernel): what PassArgs says per pass.
 struct TinyPass {
     uint32_t g0, g1, nx, q1, q2, q3, keys_fixed, pad;

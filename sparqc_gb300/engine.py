@@ -23,7 +23,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
            "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
-           "sqc_load", "sqc_fp64_rate",
+           "sqc_load", "sqc_fp64_rate", "sqc_twoq_gates", "sqc_apply_twoq",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_get_states",
@@ -67,7 +67,7 @@ class BatchOptions(ctypes.Structure):
                 ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
                 ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
                 ("memory_budget", ctypes.c_uint64), ("use_graph", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 5)]
+                ("idle_limit_us", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
 
 
 class BatchTuning(ctypes.Structure):
@@ -87,7 +87,8 @@ class ServerOptions(ctypes.Structure):
                 ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
                 ("memory_budget", ctypes.c_uint64), ("max_slots", ctypes.c_uint32), ("min_chunk", ctypes.c_uint32),
                 ("slice_ms", ctypes.c_double), ("solo_log2_groups", ctypes.c_uint32),
-                ("solo_share_pct", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+                ("solo_share_pct", ctypes.c_uint32), ("inject_alloc_failures", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
 
 
 class ServerStats(ctypes.Structure):
@@ -160,6 +161,10 @@ def load(path=LIB_PATH):
     L.sqc_stream.restype = P
     L.sqc_fp64_rate.argtypes = [U32, ctypes.POINTER(D)]
     L.sqc_fp64_rate.restype = I
+    L.sqc_twoq_gates.argtypes = [U32, U32, U32, U32, U64, D, D, P, P, U64, ctypes.POINTER(U64)]
+    L.sqc_twoq_gates.restype = I
+    L.sqc_apply_twoq.argtypes = [P, U32, U32, U32, U32, U64, D, D, P]
+    L.sqc_apply_twoq.restype = I
     L.sqc_batch_default_options.argtypes = [ctypes.POINTER(BatchOptions)]
     L.sqc_batch_default_options.restype = None
     L.sqc_batch_create.argtypes = [ctypes.POINTER(BatchOptions), ctypes.POINTER(P)]
@@ -230,6 +235,30 @@ def load(path=LIB_PATH):
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+TWOQ_UNITARY, TWOQ_RZZ, TWOQ_ISWAP, TWOQ_FSIM, TWOQ_CSWAP, TWOQ_SWAP = range(6)
+
+
+def _twoq_matrix(u):
+    if u is None:
+        return None
+    m = np.ascontiguousarray(np.asarray(u, dtype=np.complex128).reshape(4, 4)).view(np.float64)
+    return m
+
+
+def twoq_gates(form, a, b, c=0, controls=0, theta=0.0, phi=0.0, u=None):
+    """The engine's gate sequence of one two-qubit gate (a GATE_DTYPE array), for gate arrays
+    given to batches, servers or the oracle. u: the 4x4 unitary of TWOQ_UNITARY (index i_a + 2 i_b)."""
+    L = load()
+    m = _twoq_matrix(u)
+    out = np.zeros(32, GATE_DTYPE)
+    n = ctypes.c_uint64()
+    rc = L.sqc_twoq_gates(form, a, b, c, controls, theta, phi, _p(m) if m is not None else None, _p(out), out.size,
+                          ctypes.byref(n))
+    if rc != OK:
+        raise SparqcError(rc, f"sqc_twoq_gates: {L.sqc_status_string(rc).decode()}")
+    return out[:n.value].copy()
 
 
 def fp64_rate(device=0):
@@ -389,6 +418,12 @@ class State:
         return {n: getattr(s, n) for n, _ in Stats._fields_}
 
     # one-gate helpers
+    def apply_twoq(self, form, a, b, c=0, controls=0, theta=0.0, phi=0.0, u=None):
+        """One two-qubit gate (TWOQ_* form; u: the 4x4 unitary of TWOQ_UNITARY, index i_a + 2 i_b)."""
+        m = _twoq_matrix(u)
+        self._check(self._L.sqc_apply_twoq(self._h, form, a, b, c, controls, theta, phi,
+                                           _p(m) if m is not None else None), "apply_twoq")
+
     def _g(self, kind, t, controls=0, theta=0.0, phi=0.0, lam=0.0):
         g = np.zeros(1, GATE_DTYPE)
         g["kind"], g["target"], g["controls"] = kind, t, controls
@@ -436,7 +471,7 @@ class Batch:
     """
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, min_chunk=8, blocks_per_sm=0,
-                 memory_budget=0, use_graph=False, stream=None, device=0):
+                 memory_budget=0, use_graph=False, stream=None, device=0, idle_limit_us=0):
         self._L = load()
         o = BatchOptions()
         self._L.sqc_batch_default_options(ctypes.byref(o))
@@ -449,6 +484,7 @@ class Batch:
         o.use_graph = 1 if use_graph else 0
         o.stream = stream
         o.device = device
+        o.idle_limit_us = idle_limit_us
         h = ctypes.c_void_p()
         rc = self._L.sqc_batch_create(ctypes.byref(o), ctypes.byref(h))
         if rc != OK:
@@ -568,7 +604,8 @@ class Server:
     """
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, memory_budget=0, max_slots=1024,
-                 min_chunk=8, slice_ms=2.0, stream=None, device=0, solo_log2_groups=0, solo_share_pct=25):
+                 min_chunk=8, slice_ms=2.0, stream=None, device=0, solo_log2_groups=0, solo_share_pct=25,
+                 inject_alloc_failures=0):
         self._L = load()
         o = ServerOptions()
         self._L.sqc_server_default_options(ctypes.byref(o))
@@ -581,6 +618,7 @@ class Server:
         o.slice_ms = slice_ms
         o.solo_log2_groups = solo_log2_groups
         o.solo_share_pct = solo_share_pct
+        o.inject_alloc_failures = inject_alloc_failures
         o.stream = stream
         o.device = device
         h = ctypes.c_void_p()
