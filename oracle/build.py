@@ -12,7 +12,10 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("SPARQC_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $SPARQC_REFERENCE_ROOT, else a sibling directory named "reference" next
+# to this repository. Without it the host build of the reference's kernels is skipped.
+REFERENCE_ROOT = os.environ.get("SPARQC_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                           "reference")
 
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 DENSE_SO = os.path.join(BUILD, "libdense.so")

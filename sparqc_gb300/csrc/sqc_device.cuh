@@ -18,7 +18,6 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
-#include "sqc_fp64emu.cuh"
 #include "sqc_types.h"
 
 namespace sqc {
@@ -125,43 +124,18 @@ __device__ __forceinline__ long long claim_group(const TableDev& t, unsigned ep,
 // ---- arithmetic --------------------------------------------------------------------------
 // Explicit round-to-nearest operations: nothing is contracted, so every product and sum
 // rounds exactly as in the reference's source formulas (emulator/device/device_data.cuh:159-319).
-// FP64: the FP64 pipe issues two lanes per cycle per SM on this GPU, while the integer pipes
-// are many times wider; some of a formula's operations run on the integer pipes instead
-// (sqc_fp64emu.cuh, correctly rounded, so the bits are the same) and both pipes work at once.
-// SQC_FP64_EMU selects which: 0 none, 1 the second product of each pair (the s* terms and H's
-// imaginary part), 2 every product, 3 every product and sum.
-#ifndef SQC_FP64_EMU
-#define SQC_FP64_EMU 0
-#endif
 template <class T> struct Arith;
 template <> struct Arith<double> {
     __device__ static __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
     __device__ static __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
     __device__ static __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
     __device__ static __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
-    // products and sums of the update formulas, each on the pipe SQC_FP64_EMU assigns it
-    __device__ static __forceinline__ double mul_a(double a, double b) {
-        return SQC_FP64_EMU >= 2 ? emu::mul(a, b) : __dmul_rn(a, b);
-    }
-    __device__ static __forceinline__ double mul_b(double a, double b) {
-        return SQC_FP64_EMU >= 1 ? emu::mul(a, b) : __dmul_rn(a, b);
-    }
-    __device__ static __forceinline__ double add_x(double a, double b) {
-        return SQC_FP64_EMU >= 3 ? emu::add(a, b) : __dadd_rn(a, b);
-    }
-    __device__ static __forceinline__ double sub_x(double a, double b) {
-        return SQC_FP64_EMU >= 3 ? emu::sub(a, b) : __dsub_rn(a, b);
-    }
 };
 template <> struct Arith<float> {
     __device__ static __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
     __device__ static __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
     __device__ static __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
     __device__ static __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-    __device__ static __forceinline__ float mul_a(float a, float b) { return __fmul_rn(a, b); }
-    __device__ static __forceinline__ float mul_b(float a, float b) { return __fmul_rn(a, b); }
-    __device__ static __forceinline__ float add_x(float a, float b) { return __fadd_rn(a, b); }
-    __device__ static __forceinline__ float sub_x(float a, float b) { return __fsub_rn(a, b); }
 };
 
 template <class T> struct Cx { T r, i; };
@@ -270,17 +244,17 @@ __device__ __forceinline__ Cx<T> branch_update(const G& g, bool bit, Cx<T> a, Cx
         const T f = Coef<T>::c(g);
         const Cx<T> x = bit ? b : a;
         const Cx<T> y = bit ? Cx<T>{neg(a.r), neg(a.i)} : b;
-        o.r = A::mul_a(f, A::add_x(x.r, y.r));
-        o.i = A::mul_b(f, A::add_x(x.i, y.i));
+        o.r = A::mul(f, A::add(x.r, y.r));
+        o.i = A::mul(f, A::add(x.i, y.i));
     } else if constexpr (K == KRX) {
         const T c = Coef<T>::c(g), s = Coef<T>::s(g);
-        o.r = A::add_x(A::mul_a(c, a.r), A::mul_b(s, b.i));
-        o.i = A::sub_x(A::mul_a(c, a.i), A::mul_b(s, b.r));
+        o.r = A::add(A::mul(c, a.r), A::mul(s, b.i));
+        o.i = A::sub(A::mul(c, a.i), A::mul(s, b.r));
     } else if constexpr (K == KRY) {
         const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
         const T s = bit ? s0 : neg(s0);
-        o.r = A::add_x(A::mul_a(c, a.r), A::mul_b(s, b.r));
-        o.i = A::add_x(A::mul_a(c, a.i), A::mul_b(s, b.i));
+        o.r = A::add(A::mul(c, a.r), A::mul(s, b.r));
+        o.i = A::add(A::mul(c, a.i), A::mul(s, b.i));
     } else {  // KU
         const T m00r = Coef<T>::m(g, 0), m00i = Coef<T>::m(g, 1), m01r = Coef<T>::m(g, 2), m01i = Coef<T>::m(g, 3);
         const T m10r = Coef<T>::m(g, 4), m10i = Coef<T>::m(g, 5), m11r = Coef<T>::m(g, 6), m11i = Coef<T>::m(g, 7);
@@ -303,10 +277,10 @@ __device__ __forceinline__ Cx<T> diag_update(const G& g, bool bit, Cx<T> a) {
     else if constexpr (K == KRZ) {
         const T c = Coef<T>::c(g), s0 = Coef<T>::s(g);
         const T s = bit ? s0 : neg(s0);   // bit 0: conj(a)*v0, bit 1: a*v1
-        return Cx<T>{A::sub_x(A::mul_a(c, a.r), A::mul_b(s, a.i)), A::add_x(A::mul_a(c, a.i), A::mul_b(s, a.r))};
+        return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
     } else {  // KPHASE, KT, KTDG: only bit-1 amplitudes change (callers skip bit 0)
         const T c = Coef<T>::c(g), s = Coef<T>::s(g);
-        return Cx<T>{A::sub_x(A::mul_a(c, a.r), A::mul_b(s, a.i)), A::add_x(A::mul_a(c, a.i), A::mul_b(s, a.r))};
+        return Cx<T>{A::sub(A::mul(c, a.r), A::mul(s, a.i)), A::add(A::mul(c, a.i), A::mul(s, a.r))};
     }
 }
 
