@@ -338,8 +338,11 @@ __device__ __forceinline__ bool negligible(Cx<double> v, const PruneBits& t) {
     return ((unsigned long long)__double_as_longlong(v.r) & m) < t.d &&
            ((unsigned long long)__double_as_longlong(v.i) & m) < t.d;
 }
+// FP32 compares issue on the wide FP32 pipes and take |x| as an operand modifier: one compare
+// per component (NaN compares false, as its bit pattern does above t.f).
 __device__ __forceinline__ bool negligible(Cx<float> v, const PruneBits& t) {
-    return ((unsigned)__float_as_int(v.r) & 0x7FFFFFFFu) <= t.f && ((unsigned)__float_as_int(v.i) & 0x7FFFFFFFu) <= t.f;
+    const float f = __int_as_float((int)t.f);
+    return fabsf(v.r) <= f && fabsf(v.i) <= f;
 }
 
 // ---- asynchronous global -> shared copies (sm_80+ PTX) ----------------------------------
@@ -358,35 +361,5 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 // Wait until at most N of the thread's committed cp.async groups are still in flight.
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// ---- bulk global -> shared copies (cp.async.bulk) completed on an mbarrier --------------------
-// A transaction barrier in shared memory: one arrival (with the byte count the phase waits for)
-// and the bytes of the copies that signal it complete a phase.
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned arrivals) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(arrivals) : "memory");
-}
-// Makes barrier initialisations visible to the copy engine (the asynchronous proxy).
-__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-// Arrive, announcing the bytes the current phase is to receive.
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-                 ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-// True once the phase with the given parity has completed (returns after a bounded wait).
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}"
-                 : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
-    return ok != 0;
-}
-// Copy `bytes` (a multiple of 16; both addresses 16-byte aligned) from global to this CTA's shared
-// memory; the copy signals its bytes on bar.
-__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
-}
-// Orders this thread's earlier ordinary accesses to shared memory before later copy-engine ones.
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 }  // namespace sqc

@@ -13,11 +13,10 @@
 //    reference's pair rule (emulator/device/device_table_FC.cuh:62-110) lifted from keys to
 //    16-key groups, which gives the same pairs and the same per-key results. A resolve
 //    kernel settles ownership for every list entry before the pass.
-// Data movement (large tables): every warp prefetches the buckets of its next items into its
-// own ring of shared-memory slots with bulk copies (cp.async.bulk: one per 128-byte key line,
-// per amplitude line and per header, each slot's copies completing on its own mbarrier), so
-// several items are in flight while it computes; it moves the current slot into registers,
-// applies the gates and writes the results back in place with ordinary stores. Every
+// Data movement: every warp prefetches the buckets of its next slots into its own ring of
+// shared-memory slots with cp.async (16-byte copies, one commit group per slot), so several
+// slots are in flight while it computes; it moves the current slot into registers, applies
+// the gates and writes the results back in place with ordinary stores. Every
 // pair with at least one present member is read once and written once. A group that appears
 // for the first time is claimed with a 128-bit CAS and appended to the list (such groups are
 // beyond the entries the pass walks). Pruning follows the reference
@@ -352,12 +351,10 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
 
 // ---- staged pass -------------------------------------------------------------------------
 // Every warp is a worker with its own ring of D = RingDepth shared-memory slots. It copies the
-// buckets of the item D-1 steps ahead into its slot with bulk copies (lane k of the first NB
-// lanes copies bucket k's key line, lane NB + k its amplitude line, lane 2 NB + k its header),
-// whose bytes complete the slot's mbarrier phase; it waits for the current slot's phase, moves
-// the slot into registers, applies the gates and writes back in place. A slot holds the
-// buckets of one item: four list entries (stream pass), two owned pairs (pair pass), one owned
-// quad, or one owned octet (eight buckets).
+// buckets of the slot D-1 steps ahead with cp.async (one commit group per slot), waits
+// for the current slot's group, moves the slot into registers, applies the gates and writes
+// back in place. A slot holds the buckets of one item: four list entries (stream pass), two
+// owned pairs (pair pass), one owned quad, or one owned octet (eight buckets).
 constexpr int kWarpsPerBlock = 4;
 constexpr int kStagedThreads = 32 * kWarpsPerBlock;
 // FP32 octet rings hold three slots (two items in flight, 27 KB per block): the same six
@@ -374,8 +371,7 @@ template <class T, int NB> struct Slot {
     unsigned long long G[NB];   // pair passes: group of each held bucket
     unsigned int b[NB];         // bucket index, kNoBucket when absent
     int n;                      // 0: nothing more for this warp
-    int pad;
-    unsigned long long bar;     // mbarrier: the slot's copies have landed
+    int pad[3];
 };
 template <int NX> struct SlotBuckets { static constexpr int kN = NX == 3 ? 8 : 4; };
 
@@ -437,49 +433,62 @@ __device__ __forceinline__ void fetch_item(SlotSource& src, const TableDev& t, u
     }
 }
 
-// Copy the prefetched item's buckets into a ring slot (bulk copies completing on the slot's
-// mbarrier; lane 0 announces their byte count) and prefetch the next item. The slot's previous
-// contents were moved to registers by every lane before the warp barrier that ended that step.
+// Copy the prefetched item's buckets into a ring slot (cp.async, one commit group) and
+// prefetch the next item.
 template <class T, int NX>
 __device__ __forceinline__ void issue_slot(Slot<T, SlotBuckets<NX>::kN>& sl, const TableDev& t, SlotSource& src,
                                            unsigned long long n, unsigned long long units, unsigned long long m1,
                                            unsigned long long m2, unsigned long long m3, int lane) {
     constexpr int NB = SlotBuckets<NX>::kN;
-    constexpr unsigned kAmp = (unsigned)(sizeof(typename AmpT<T>::V) * kSlots);
-    constexpr int kRoles = NX ? 2 : 3;   // key line, amplitude line (, header)
+    constexpr uint32_t kAmp = (uint32_t)(sizeof(typename AmpT<T>::V) * kSlots);
+    constexpr int kKeyChunks = 128 / 16, kAmpChunks = (int)(kAmp / 16);
+    constexpr int kChunks = NB * (kKeyChunks + kAmpChunks) + (NX ? 0 : 4);
     const unsigned bk = src.nb;
     const unsigned long long Gk = src.ng;
     const bool any = src.nany;
     fetch_item<NX>(src, t, n, units, m1, m2, m3, lane);
+    const unsigned b0 = __shfl_sync(kFull, bk, 0), b1 = __shfl_sync(kFull, bk, 1);
+    const unsigned b2 = __shfl_sync(kFull, bk, 2), b3 = __shfl_sync(kFull, bk, 3);
+    unsigned b4 = kNoBucket, b5 = kNoBucket, b6 = kNoBucket, b7 = kNoBucket;
+    if constexpr (NB == 8) {
+        b4 = __shfl_sync(kFull, bk, 4); b5 = __shfl_sync(kFull, bk, 5);
+        b6 = __shfl_sync(kFull, bk, 6); b7 = __shfl_sync(kFull, bk, 7);
+    }
     if (lane < NB) {
         sl.b[lane] = bk;
         sl.G[lane] = Gk;
     }
     if (lane == 0) sl.n = any ? 1 : 0;
-    const unsigned present = __ballot_sync(kFull, lane < NB && bk != kNoBucket);
-    const int k = lane % NB, role = lane / NB;
-    const unsigned b = __shfl_sync(kFull, bk, k);
-    fence_proxy_async_smem();   // the copies' writes come after this warp's earlier reads of the slot
-    if (lane == 0) mbar_arrive_expect_tx(&sl.bar, (unsigned)__popc(present) * (128u + kAmp + (NX ? 0u : 16u)));
-    if (role < kRoles && b != kNoBucket) {
-        if (role == 0) bulk_copy_g2s(sl.keys[k], t.keys + (size_t)b * kSlots, 128u, &sl.bar);
-        else if (role == 1) bulk_copy_g2s(sl.amps[k], reinterpret_cast<const char*>(t.amps) + (size_t)b * kAmp, kAmp, &sl.bar);
-        else bulk_copy_g2s(&sl.hdr[k], t.hdr + b, 16u, &sl.bar);
+    for (int c = lane; c < kChunks; c += 32) {
+        int k, off;
+        const char* s;
+        char* d;
+        if (c < NB * kKeyChunks) {
+            k = c / kKeyChunks; off = (c % kKeyChunks) * 16;
+        } else if (c < NB * (kKeyChunks + kAmpChunks)) {
+            const int x = c - NB * kKeyChunks;
+            k = x / kAmpChunks; off = (x % kAmpChunks) * 16;
+        } else {
+            k = c - NB * (kKeyChunks + kAmpChunks); off = 0;
+        }
+        const unsigned b = k < 4 ? (k == 0 ? b0 : k == 1 ? b1 : k == 2 ? b2 : b3)
+                                 : (k == 4 ? b4 : k == 5 ? b5 : k == 6 ? b6 : b7);
+        if (b == kNoBucket) continue;
+        if (c < NB * kKeyChunks) {
+            s = reinterpret_cast<const char*>(t.keys + (size_t)b * kSlots) + off;
+            d = reinterpret_cast<char*>(sl.keys[k]) + off;
+        } else if (c < NB * (kKeyChunks + kAmpChunks)) {
+            s = reinterpret_cast<const char*>(t.amps) + (size_t)b * kAmp + off;
+            d = reinterpret_cast<char*>(sl.amps[k]) + off;
+        } else {
+            s = reinterpret_cast<const char*>(t.hdr + b);
+            d = reinterpret_cast<char*>(&sl.hdr[k]);
+        }
+        cp_async16(d, s);
     }
+    cp_async_commit();
 }
 
-// Wait for phase `parity` of a slot's copies, bounded: false (and ST_TIMEOUT) when they have not
-// landed after about a second; the warp then waits once more, bounded again, for the copies it
-// issued and ends its pass.
-constexpr unsigned kCopyWaitIters = 1u << 20;
-__device__ __forceinline__ bool wait_slot(unsigned long long* bar, unsigned parity, Ctl* ctl, int lane) {
-    for (unsigned i = 0; i < kCopyWaitIters; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    if (lane == 0) atomicCAS(&ctl->status, 0u, (unsigned)ST_TIMEOUT);
-    for (unsigned i = 0; i < kCopyWaitIters; ++i)
-        if (mbar_try_wait(bar, parity)) break;
-    return false;
-}
 
 template <class T, int NX>
 __global__ void __launch_bounds__(kStagedThreads, StagedOcc<T, NX>::kMin) staged_kernel(PassArgs a) {
@@ -508,16 +517,11 @@ __global__ void __launch_bounds__(kStagedThreads, StagedOcc<T, NX>::kMin) staged
     src.count = NX == 0 ? (n + 3) / 4 : NX == 1 ? (units + 1) / 2 : units;
     fetch_item<NX>(src, t, n, units, m1, m2, m3, lane);
     unsigned long long cnt_nnz = 0, cnt_empty = 0, upd = 0;
-    if (lane == 0)
-        for (int d = 0; d < D; ++d) mbar_init(&ring[d].bar, 1);
-    mbar_init_fence();
-    __syncwarp();
     for (int d = 0; d < D - 1; ++d) issue_slot<T, NX>(ring[d], t, src, n, units, m1, m2, m3, lane);
     Val<T> va, vb;
     for (unsigned step = 0;; ++step) {
         issue_slot<T, NX>(ring[(step + D - 1) % D], t, src, n, units, m1, m2, m3, lane);
-        // item `step` is the (step / D)-th fill of its slot: that phase's parity
-        if (!wait_slot(&ring[step % D].bar, (step / D) & 1u, ctl, lane)) break;
+        cp_async_wait<D - 1>();
         __syncwarp();
         const Slot<T, NB>& sl = ring[step % D];
         if (sl.n == 0) break;
@@ -557,8 +561,7 @@ __global__ void __launch_bounds__(kStagedThreads, StagedOcc<T, NX>::kMin) staged
         const long long fb = write_val<T>(t, ep, vb, lane, &ctl->status, cnt_nnz, cnt_empty);
         if (NX) append_new(t, ctl, fa, fb, lane);
     }
-    // no copy is in flight here: every item after the one that ended the loop lies beyond the
-    // pass's items and copied nothing
+    cp_async_wait<0>();   // nothing may still be landing in shared memory when the block exits
     finish_pass(ctl, cnt_nnz, cnt_empty, upd, nnz_in, a.keys_fixed != 0, NX > 0, a.amp_bytes);
 }
 

@@ -78,6 +78,15 @@ __device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long k
 // still forms it, for the warp vote that skips FP64 work no lane needs.
 template <class T> struct NeedAny { static constexpr bool kOn = Vote<T>::kSkip; };
 
+// The per-slot steps below update a slot with selects on the per-lane conditions (controls,
+// presence) rather than branches around them: the warp runs the arithmetic once for all its
+// lanes either way, and the selects spare the divergent branches. Only the FP64 warp vote
+// (warp_needs) branches, and it is uniform across the warp.
+template <class T>
+__device__ __forceinline__ Cx<T> pick(bool c, Cx<T> x, Cx<T> y) {
+    return Cx<T>{c ? x.r : y.r, c ? x.i : y.i};
+}
+
 // A branching or swap gate of kind K whose partner slot sits in lane ^ off; bit is the slot's
 // logical target bit.
 template <class T, uint32_t K, class G>
@@ -91,22 +100,19 @@ __device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off
     bool pp = false;
     if (swap || NeedAny<T>::kOn) pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;   // warp-uniform
     if (swap) {
-        if (sat) {
-            v.amp = K == KANY ? swap_update_rt<T>(h.kind, bit, pa) : swap_update<T, K == KANY ? KX : K>(bit, pa);
-            v.pres = pp;
-            v.dirty = true;
-        }
+        const Cx<T> o = K == KANY ? swap_update_rt<T>(h.kind, bit, pa) : swap_update<T, K == KANY ? KX : K>(bit, pa);
+        v.amp = pick(sat, o, v.amp);
+        v.pres = sat ? pp : v.pres;
+        v.dirty = v.dirty || sat;
     } else {
         const bool any = !NeedAny<T>::kOn || v.pres || pp;
         if (warp_needs<T>(sat && any)) {
             const Cx<T> o = K == KANY ? branch_update_rt<T>(h.kind, g, bit, v.amp, pa)
                                       : branch_update<T, K == KANY ? KH : K>(g, bit, v.amp, pa);
-            if (sat) {
-                const bool keep = any && !negligible(o, pb);
-                v.pres = keep;
-                v.amp = keep ? o : czero<T>();
-                v.dirty = true;
-            }
+            const bool keep = any && !negligible(o, pb);
+            v.amp = pick(sat, pick(keep, o, czero<T>()), v.amp);
+            v.pres = sat ? keep : v.pres;
+            v.dirty = v.dirty || sat;
         }
     }
 }
@@ -123,7 +129,8 @@ __device__ __forceinline__ void diag_step(const G& g, const GateHead& h, Val<T>&
         if constexpr (K == KS) {   // Sdg runs S's code: its result is S's negated (exact)
             if (h.kind == KSDG) o = Cx<T>{neg(o.r), neg(o.i)};
         }
-        if (need) { v.amp = o; v.dirty = true; }
+        v.amp = pick(need, o, v.amp);
+        v.dirty = v.dirty || need;
     }
 }
 
@@ -137,14 +144,15 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
     const bool swap = K == KANY ? (h.op & kOpSwap) != 0 : swap_kind(K);
     constexpr uint32_t KS_ = K == KANY ? KX : K;
     if (swap) {
-        if (sat) {
-            const Cx<T> na = K == KANY ? swap_update_rt<T>(h.kind, bit_a, b.amp) : swap_update<T, KS_>(bit_a, b.amp);
-            const Cx<T> nb = K == KANY ? swap_update_rt<T>(h.kind, bit_b, a.amp) : swap_update<T, KS_>(bit_b, a.amp);
-            const bool pa = b.pres, pbr = a.pres;
-            a.amp = na; b.amp = nb;
-            a.pres = pa; b.pres = pbr;
-            a.dirty = b.dirty = true;
-        }
+        const Cx<T> na = K == KANY ? swap_update_rt<T>(h.kind, bit_a, b.amp) : swap_update<T, KS_>(bit_a, b.amp);
+        const Cx<T> nb = K == KANY ? swap_update_rt<T>(h.kind, bit_b, a.amp) : swap_update<T, KS_>(bit_b, a.amp);
+        const bool pa = b.pres, pbr = a.pres;
+        a.amp = pick(sat, na, a.amp);
+        b.amp = pick(sat, nb, b.amp);
+        a.pres = sat ? pa : a.pres;
+        b.pres = sat ? pbr : b.pres;
+        a.dirty = a.dirty || sat;
+        b.dirty = b.dirty || sat;
     } else {
         const bool any = !NeedAny<T>::kOn || a.pres || b.pres;
         if (warp_needs<T>(sat && any)) {
@@ -153,12 +161,13 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
                                        : branch_update<T, KB_>(g, bit_a, a.amp, b.amp);
             const Cx<T> ob = K == KANY ? branch_update_rt<T>(h.kind, g, bit_b, b.amp, a.amp)
                                        : branch_update<T, KB_>(g, bit_b, b.amp, a.amp);
-            if (sat) {
-                const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
-                a.pres = ka; a.amp = ka ? oa : czero<T>();
-                b.pres = kb; b.amp = kb ? ob : czero<T>();
-                a.dirty = b.dirty = true;
-            }
+            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+            a.amp = pick(sat, pick(ka, oa, czero<T>()), a.amp);
+            b.amp = pick(sat, pick(kb, ob, czero<T>()), b.amp);
+            a.pres = sat ? ka : a.pres;
+            b.pres = sat ? kb : b.pres;
+            a.dirty = a.dirty || sat;
+            b.dirty = b.dirty || sat;
         }
     }
 }
@@ -205,21 +214,22 @@ __device__ __forceinline__ void gate_on(const G& g, const GateHead& h, Val<T>& a
 // branching and swap gates on the pass's first cross-group qubit pair a with b (lane-local),
 // those on qubits 0..3 or on the second cross-group qubit pair each lane with lane ^ off (the
 // other half of the warp holds the groups with the second qubit's bit set), diagonal gates are
-// lane-local. Lane 0 accumulates the amp-update count: every gate is credited with the present
-// slots it sees, and host-resolved gates recorded in a descriptor's credit with the same count.
+// lane-local. Every lane accumulates the amp-update count of its own slots (the pass sums the
+// lanes): every gate is credited with the present slots it sees, and host-resolved gates
+// recorded in a descriptor's credit with the same count.
 template <class T, bool SPEC = true>
 __device__ __forceinline__ void run_gates(const GateDesc* __restrict__ gates, uint32_t g0, uint32_t g1, Val<T>& a,
                                           Val<T>& b, int lane, const PruneBits& pb, unsigned long long& upd) {
     // present slots in the warp: only a branching gate changes the count (swap gates permute
     // presence among slots that satisfy the same controls, diagonal gates keep it)
-    unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+    unsigned n = (unsigned)a.pres + (unsigned)b.pres;
     bool recount = false;
     for (uint32_t gi = g0; gi < g1; ++gi) {
         const GateDesc* g = gates + gi;
         const GateHead h = gate_head(g);
-        if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        if (recount) n = (unsigned)a.pres + (unsigned)b.pres;
         recount = (h.op & kOpBranch) != 0;
-        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        upd += (unsigned long long)n * (1ULL + h.credit);
         if constexpr (!SPEC) {
             gate_on<T, KANY>(g, h, a, b, pb);
             continue;
@@ -298,7 +308,7 @@ template <class T, bool SPEC = true>
 __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* __restrict__ gates, uint32_t g0,
                                             uint32_t g1, Val<T>& a, Val<T>& b, int lane, const PruneBits& pb,
                                             unsigned long long& upd) {
-    unsigned n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+    unsigned n = (unsigned)a.pres + (unsigned)b.pres;
     bool recount = false;
     for (uint32_t gi = g0; gi < g1; ++gi) {
         const SmemGate& x = sg[gi - g0];
@@ -311,9 +321,9 @@ __device__ __forceinline__ void run_gates_s(const SmemGate* sg, const GateDesc* 
         h.op = v1.z;
         h.credit = v1.w;
         const SmemCoef<T> g = SmemPair<T>::of(x, gates + gi);
-        if (recount) n = __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres));
+        if (recount) n = (unsigned)a.pres + (unsigned)b.pres;
         recount = (h.op & kOpBranch) != 0;
-        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        upd += (unsigned long long)n * (1ULL + h.credit);
         if constexpr (!SPEC) {
             gate_on<T, KANY>(g, h, a, b, pb);
             continue;
@@ -549,8 +559,7 @@ __device__ __forceinline__ void gate_on4(const G& g, const GateHead& h, Val<T>& 
 
 template <class T>
 __device__ __forceinline__ unsigned present4(const Val<T>& a, const Val<T>& b, const Val<T>& c, const Val<T>& d) {
-    return __popc(__ballot_sync(kFull, a.pres)) + __popc(__ballot_sync(kFull, b.pres)) +
-           __popc(__ballot_sync(kFull, c.pres)) + __popc(__ballot_sync(kFull, d.pres));
+    return (unsigned)a.pres + (unsigned)b.pres + (unsigned)c.pres + (unsigned)d.pres;
 }
 
 // Gates [g0, g1) on the lane's four slots (from shared memory with SMEM, sg[i] = gate g0 + i).
@@ -576,7 +585,7 @@ __device__ __forceinline__ void run_gates4(const SmemGate* sg, const GateDesc* _
         }
         if (recount) n = present4(a, b, c, d);
         recount = (h.op & kOpBranch) != 0;
-        if (lane == 0) upd += (unsigned long long)n * (1ULL + h.credit);
+        upd += (unsigned long long)n * (1ULL + h.credit);
         auto go = [&](const auto& g) {
             switch (h.kind) {
             case KX: gate_on4<T, KX>(g, h, a, b, c, d, pb); break;
