@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--impl", default="sparqc", choices=["sparqc", "reference"])
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-fp32", action="store_true", help="c1-c3 FP64: skip the FP32 run of the same circuit")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default line: skip the batching and serving summaries (keys c4, c5)")
     ap.add_argument("--circuits", type=int, default=256, help="c4: circuits per batch")
     ap.add_argument("--autotune", action="store_true", help="c4: autotune the batch before timing")
     ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
@@ -480,6 +482,12 @@ def run_gpu(args):
                 "passes_per_step": (q1["passes"] - q0["passes"]) / args.steps, "fidelity_vs_fp64": fid32, "max_abs_err_vs_fp64": err32}
         s32.close()
 
+    extras = {}
+    if not args.no_extras and world == 1 and args.workload == "c3" and args.k is None and args.gates is None:
+        from sparqc_gb300 import circuits as circ
+        extras["c4"] = batch_summary(engine, circ, stream, args.steps, flush)
+        extras["c5"] = serve_summary(engine, circ, stream)
+
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -512,6 +520,7 @@ def run_gpu(args):
                                   "note": "gates applied on the device only; `value` also credits the gates the "
                                           "host resolved without touching the state, as the reference runs them"},
            "fp32": fp32}
+    out.update(extras)
     print(json.dumps(out), flush=True)
     st.close()
 
@@ -653,6 +662,71 @@ def run_batch(args):
            "passes_per_step": s1["passes"], "table_bytes": s1["table_bytes"]}
     print(json.dumps(out), flush=True)
     b.close()
+
+
+def batch_summary(engine, circuits, stream, steps, flush):
+    """The batching configuration (256 circuits, FP32, one persistent launch, graph replay) next to
+    the plain per-circuit FP64 path on the same circuits, for the default line."""
+    import torch
+    cs = [(nq, g) for nq, _, g in circuits.batch_circuits(256, seed=0)]
+    b = engine.Batch(precision=32, use_graph=True, stream=stream.cuda_stream)
+    b.prepare(cs)
+    for _ in range(3):
+        b.run()
+        b.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        b.run()
+        ev[i][1].record(stream)
+    b.sync()
+    ms = sum(x.elapsed_time(y) for x, y in ev) / steps
+    b64 = engine.Batch(precision=64, stream=stream.cuda_stream)
+    b64.prepare(cs)
+    b64.run()
+    b64.sync()
+    fids = [fidelity(b.state(i), b64.state(i))[0] for i in range(len(cs))]
+    b.close()
+    b64.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for nq, g in cs:
+        st = engine.State(nq, stream=stream.cuda_stream)
+        st.apply(g)
+        st.sync()
+        st.close()
+    plain_t = time.perf_counter() - t0
+    return {"workload": "c4: 256 circuits, qubits 16-48, k 8-18, depth 100-1000, FP32, one persistent launch",
+            "circuits_per_s": len(cs) / (ms / 1e3), "ms_per_batch": ms,
+            "plain_fp64_circuits_per_s": len(cs) / plain_t,
+            "speedup_vs_plain_fp64": (len(cs) / (ms / 1e3)) / (len(cs) / plain_t),
+            "fp32_min_fidelity_vs_fp64": min(fids)}
+
+
+def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
+    """The serving configuration at one saturating arrival rate, FP32, next to the plain per-circuit
+    FP64 path over the same requests back to back, for the default line."""
+    import torch
+    reqs = circuits.serving_stream(requests, rate, seed=0)
+    lat, makespan, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0)
+    lat = np.array(lat)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _, nq, _, g in reqs:
+        st = engine.State(nq, stream=stream.cuda_stream)
+        st.apply(g)
+        st.sync()
+        st.close()
+    plain_t = time.perf_counter() - t0
+    served = len(reqs) / makespan
+    return {"workload": f"c5: {requests} Poisson arrivals at {rate:g}/s of c4 circuits plus 5% large "
+                        "(48 qubits, k=24, 2000 gates), 120 GB budget, 2 ms slices, FP32",
+            "circuits_per_s": served, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+            "plain_fp64_circuits_per_s": len(reqs) / plain_t, "speedup_vs_plain_fp64": served / (len(reqs) / plain_t),
+            "large": int(sum(1 for r in reqs if r[2] == 24))}
 
 
 # --------------------------------------------------------------------------------------

@@ -78,10 +78,14 @@ __device__ __forceinline__ bool slot_bit(const GateHead& h, unsigned long long k
 // still forms it, for the warp vote that skips FP64 work no lane needs.
 template <class T> struct NeedAny { static constexpr bool kOn = Vote<T>::kSkip; };
 
-// The per-slot steps below update a slot with selects on the per-lane conditions (controls,
-// presence) rather than branches around them: the warp runs the arithmetic once for all its
-// lanes either way, and the selects spare the divergent branches. Only the FP64 warp vote
-// (warp_needs) branches, and it is uniform across the warp.
+// FP64 steps update a slot with selects on the per-lane conditions (controls, presence)
+// rather than branches around them: the warp runs the arithmetic once for all its lanes either
+// way, and the selects spare the divergent branches (64-qubit FP64 workload 0.6% faster).
+// FP32 steps keep the branches: their selects made the octet kernels' code larger, and the
+// instruction-fetch stalls cost more than the branches (64-qubit FP32 workload 3% slower).
+// Only the FP64 warp vote (warp_needs) branches in the select form, uniformly across the warp.
+template <class T> struct SelectForm { static constexpr bool kOn = sizeof(T) == 8; };
+
 template <class T>
 __device__ __forceinline__ Cx<T> pick(bool c, Cx<T> x, Cx<T> y) {
     return Cx<T>{c ? x.r : y.r, c ? x.i : y.i};
@@ -101,18 +105,31 @@ __device__ __forceinline__ void shfl_step(const G& g, const GateHead& h, int off
     if (swap || NeedAny<T>::kOn) pp = __shfl_xor_sync(kFull, (int)v.pres, off) != 0;   // warp-uniform
     if (swap) {
         const Cx<T> o = K == KANY ? swap_update_rt<T>(h.kind, bit, pa) : swap_update<T, K == KANY ? KX : K>(bit, pa);
-        v.amp = pick(sat, o, v.amp);
-        v.pres = sat ? pp : v.pres;
-        v.dirty = v.dirty || sat;
+        if constexpr (SelectForm<T>::kOn) {
+            v.amp = pick(sat, o, v.amp);
+            v.pres = sat ? pp : v.pres;
+            v.dirty = v.dirty || sat;
+        } else if (sat) {
+            v.amp = o;
+            v.pres = pp;
+            v.dirty = true;
+        }
     } else {
         const bool any = !NeedAny<T>::kOn || v.pres || pp;
         if (warp_needs<T>(sat && any)) {
             const Cx<T> o = K == KANY ? branch_update_rt<T>(h.kind, g, bit, v.amp, pa)
                                       : branch_update<T, K == KANY ? KH : K>(g, bit, v.amp, pa);
-            const bool keep = any && !negligible(o, pb);
-            v.amp = pick(sat, pick(keep, o, czero<T>()), v.amp);
-            v.pres = sat ? keep : v.pres;
-            v.dirty = v.dirty || sat;
+            if constexpr (SelectForm<T>::kOn) {
+                const bool keep = any && !negligible(o, pb);
+                v.amp = pick(sat, pick(keep, o, czero<T>()), v.amp);
+                v.pres = sat ? keep : v.pres;
+                v.dirty = v.dirty || sat;
+            } else if (sat) {
+                const bool keep = any && !negligible(o, pb);
+                v.pres = keep;
+                v.amp = keep ? o : czero<T>();
+                v.dirty = true;
+            }
         }
     }
 }
@@ -129,8 +146,13 @@ __device__ __forceinline__ void diag_step(const G& g, const GateHead& h, Val<T>&
         if constexpr (K == KS) {   // Sdg runs S's code: its result is S's negated (exact)
             if (h.kind == KSDG) o = Cx<T>{neg(o.r), neg(o.i)};
         }
-        v.amp = pick(need, o, v.amp);
-        v.dirty = v.dirty || need;
+        if constexpr (SelectForm<T>::kOn) {
+            v.amp = pick(need, o, v.amp);
+            v.dirty = v.dirty || need;
+        } else if (need) {
+            v.amp = o;
+            v.dirty = true;
+        }
     }
 }
 
@@ -147,12 +169,18 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
         const Cx<T> na = K == KANY ? swap_update_rt<T>(h.kind, bit_a, b.amp) : swap_update<T, KS_>(bit_a, b.amp);
         const Cx<T> nb = K == KANY ? swap_update_rt<T>(h.kind, bit_b, a.amp) : swap_update<T, KS_>(bit_b, a.amp);
         const bool pa = b.pres, pbr = a.pres;
-        a.amp = pick(sat, na, a.amp);
-        b.amp = pick(sat, nb, b.amp);
-        a.pres = sat ? pa : a.pres;
-        b.pres = sat ? pbr : b.pres;
-        a.dirty = a.dirty || sat;
-        b.dirty = b.dirty || sat;
+        if constexpr (SelectForm<T>::kOn) {
+            a.amp = pick(sat, na, a.amp);
+            b.amp = pick(sat, nb, b.amp);
+            a.pres = sat ? pa : a.pres;
+            b.pres = sat ? pbr : b.pres;
+            a.dirty = a.dirty || sat;
+            b.dirty = b.dirty || sat;
+        } else if (sat) {
+            a.amp = na; b.amp = nb;
+            a.pres = pa; b.pres = pbr;
+            a.dirty = b.dirty = true;
+        }
     } else {
         const bool any = !NeedAny<T>::kOn || a.pres || b.pres;
         if (warp_needs<T>(sat && any)) {
@@ -161,13 +189,20 @@ __device__ __forceinline__ void pair_step(const G& g, const GateHead& h, Val<T>&
                                        : branch_update<T, KB_>(g, bit_a, a.amp, b.amp);
             const Cx<T> ob = K == KANY ? branch_update_rt<T>(h.kind, g, bit_b, b.amp, a.amp)
                                        : branch_update<T, KB_>(g, bit_b, b.amp, a.amp);
-            const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
-            a.amp = pick(sat, pick(ka, oa, czero<T>()), a.amp);
-            b.amp = pick(sat, pick(kb, ob, czero<T>()), b.amp);
-            a.pres = sat ? ka : a.pres;
-            b.pres = sat ? kb : b.pres;
-            a.dirty = a.dirty || sat;
-            b.dirty = b.dirty || sat;
+            if constexpr (SelectForm<T>::kOn) {
+                const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+                a.amp = pick(sat, pick(ka, oa, czero<T>()), a.amp);
+                b.amp = pick(sat, pick(kb, ob, czero<T>()), b.amp);
+                a.pres = sat ? ka : a.pres;
+                b.pres = sat ? kb : b.pres;
+                a.dirty = a.dirty || sat;
+                b.dirty = b.dirty || sat;
+            } else if (sat) {
+                const bool ka = any && !negligible(oa, pb), kb = any && !negligible(ob, pb);
+                a.pres = ka; a.amp = ka ? oa : czero<T>();
+                b.pres = kb; b.amp = kb ? ob : czero<T>();
+                a.dirty = b.dirty = true;
+            }
         }
     }
 }
