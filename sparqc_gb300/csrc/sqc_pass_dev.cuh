@@ -30,7 +30,7 @@ __device__ __forceinline__ bool slot_present(unsigned long long key, int j) { re
 // lives (b = -1 for a group absent at the start of the pass) and whether the pass changed it.
 template <class T> struct Val {
     unsigned long long key;
-    long long b;
+    int b;   // bucket index (< 2^31: far more buckets than any device holds), -1 when absent
     Cx<T> amp;
     bool pres, pres0, dirty;
 };
