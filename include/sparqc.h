@@ -278,7 +278,11 @@ typedef struct sqc_batch_options {
     uint32_t idle_limit_us;    /* a warp of the persistent kernel that finds no work for this long
                                   ends the run, which then fails with SQC_ERR_STATE (every wait in
                                   the kernel is bounded); 0 = 2 s */
-    uint32_t reserved[4];
+    uint32_t threads_per_unit; /* threads that hold one unit of a pass pairing 16-key groups: 16 (a
+                                  pair of groups per half-warp: one qubit >= 4 per pass) or 32 (a
+                                  quad per warp: two qubits >= 4 per pass); 0 = 32. Results do not
+                                  depend on it; sqc_batch_autotune picks it */
+    uint32_t reserved[3];
 } sqc_batch_options;
 
 /* Tuning picked by sqc_batch_autotune. */
@@ -289,7 +293,7 @@ typedef struct sqc_batch_tuning {
     double best_ms;            /* run time of the chosen tuning */
     double default_ms;         /* run time of the tuning in effect before the call */
     uint32_t candidates;       /* tunings timed */
-    uint32_t reserved;
+    uint32_t threads_per_unit; /* 16 (pair units) or 32 (quad units), see sqc_batch_options */
 } sqc_batch_tuning;
 
 typedef struct sqc_batch_stats {

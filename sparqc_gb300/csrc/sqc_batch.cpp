@@ -129,6 +129,9 @@ int Batch::init(const sqc_batch_options* opt) {
     min_chunk_ = o.min_chunk;
     blocks_per_sm_ = o.blocks_per_sm;
     idle_limit_ns_ = o.idle_limit_us ? 1000ULL * o.idle_limit_us : 2000000000ULL;
+    if (o.threads_per_unit != 0 && o.threads_per_unit != 16 && o.threads_per_unit != 32)
+        return fail(SQC_ERR_ARG, "threads_per_unit must be 0, 16 or 32");
+    max_nx_ = o.threads_per_unit == 16 ? 1u : 2u;
     use_graph_ = o.use_graph != 0;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
@@ -165,11 +168,27 @@ void Batch::drop_graph() {
 
 int Batch::prepare(const sqc_circuit_desc* cs, uint32_t n) {
     if (n && !cs) return fail(SQC_ERR_ARG, "null circuit array");
+    std::vector<uint32_t> nqs(n);
+    std::vector<std::vector<sqc_gate>> gates(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (cs[i].n_gates && !cs[i].gates) return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": null gates");
+        nqs[i] = cs[i].nq;
+        gates[i].assign(cs[i].gates, cs[i].gates + cs[i].n_gates);
+    }
+    nqs_.swap(nqs);
+    gates_.swap(gates);
+    return plan_and_upload();
+}
+
+// Plan the stored circuits with the current pass layout (max_nx_), upload descriptors and
+// passes, and lay out the slices.
+int Batch::plan_and_upload() {
+    const uint32_t n = (uint32_t)gates_.size();
     int rc;
     if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
     std::vector<CircuitPlan> plans(n);
     for (uint32_t i = 0; i < n; ++i) {
-        if (const char* why = plan_circuit(cs[i].nq, cs[i].gates, cs[i].n_gates, kMaxRun, 2, &plans[i]))
+        if (const char* why = plan_circuit(nqs_[i], gates_[i].data(), gates_[i].size(), kMaxRun, max_nx_, &plans[i]))
             return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": " + why);
     }
     plans_.swap(plans);
@@ -539,12 +558,13 @@ int Batch::stats(sqc_batch_stats* out) {
     return SQC_OK;
 }
 
-// Time each candidate tuning (two runs each, the faster counts) and keep the fastest. The
-// load factor changes the slice layout; chunk size and blocks per SM only the launch.
+// Time each candidate tuning (two runs each, the faster counts) and keep the fastest. Threads
+// per unit (pair or quad units: one or two qubits >= 4 per pass) changes the circuits' passes,
+// the load factor the slice layout; chunk size and blocks per SM only the launch.
 int Batch::autotune(sqc_batch_tuning* out) {
     if (plans_.empty()) return fail(SQC_ERR_STATE, "no circuits prepared");
     const double lf0 = lf_;
-    const uint32_t ch0 = min_chunk_, bps0 = blocks_per_sm_;
+    const uint32_t ch0 = min_chunk_, bps0 = blocks_per_sm_, nx0 = max_nx_;
     int rc;
     auto time_it = [&](double* ms) -> int {
         double best = 1e300;
@@ -559,31 +579,44 @@ int Batch::autotune(sqc_batch_tuning* out) {
     double def_ms = 0;
     if ((rc = time_it(&def_ms))) return rc;
     double best_ms = def_ms, best_lf = lf0;
-    uint32_t best_ch = ch0, best_bps = bps0;
+    uint32_t best_ch = ch0, best_bps = bps0, best_nx = nx0;
     uint32_t count = 1;
     const int res = std::max(batch_residency(dbl_, 0), batch_residency(dbl_, 2));
-    for (double lf : {0.45, 0.25}) {
-        lf_ = lf;
-        if ((rc = layout())) {
-            if (rc == SQC_ERR_BUDGET) continue;
-            return rc;
+    for (uint32_t nx : {2u, 1u}) {
+        if (nx != max_nx_) {
+            max_nx_ = nx;
+            if ((rc = plan_and_upload())) return rc;
         }
-        for (uint32_t ch : {4u, 8u, 16u, 32u}) {
-            for (int bps = 1; bps <= res; ++bps) {
-                min_chunk_ = ch;
-                blocks_per_sm_ = (uint32_t)bps;
-                drop_graph();
-                double ms = 0;
-                if ((rc = time_it(&ms))) return rc;
-                ++count;
-                if (ms < best_ms) { best_ms = ms; best_lf = lf; best_ch = ch; best_bps = (uint32_t)bps; }
+        for (double lf : {0.45, 0.25}) {
+            lf_ = lf;
+            if ((rc = layout())) {
+                if (rc == SQC_ERR_BUDGET) continue;
+                return rc;
+            }
+            for (uint32_t ch : {4u, 8u, 16u, 32u}) {
+                for (int bps = 1; bps <= res; ++bps) {
+                    min_chunk_ = ch;
+                    blocks_per_sm_ = (uint32_t)bps;
+                    drop_graph();
+                    double ms = 0;
+                    if ((rc = time_it(&ms))) return rc;
+                    ++count;
+                    if (ms < best_ms) {
+                        best_ms = ms; best_lf = lf; best_ch = ch; best_bps = (uint32_t)bps; best_nx = nx;
+                    }
+                }
             }
         }
     }
     lf_ = best_lf;
     min_chunk_ = best_ch;
     blocks_per_sm_ = best_bps;
-    if ((rc = layout())) return rc;   // also drops a captured graph
+    if (best_nx != max_nx_) {
+        max_nx_ = best_nx;
+        if ((rc = plan_and_upload())) return rc;   // plans, uploads and lays out the slices
+    } else if ((rc = layout())) {
+        return rc;   // also drops a captured graph
+    }
     if ((rc = run()) || (rc = sync())) return rc;
     if (out) {
         std::memset(out, 0, sizeof *out);
@@ -593,6 +626,7 @@ int Batch::autotune(sqc_batch_tuning* out) {
         out->best_ms = best_ms;
         out->default_ms = def_ms;
         out->candidates = count;
+        out->threads_per_unit = best_nx == 1 ? 16u : 32u;
     }
     return SQC_OK;
 }

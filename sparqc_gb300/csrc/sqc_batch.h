@@ -79,6 +79,7 @@ private:
     int fail(int code, const std::string& msg);
     int cuda(cudaError_t e, const char* what);
     int layout();                   // slices for the current plans and tuning
+    int plan_and_upload();          // plans of the stored circuits (max_nx_), uploaded, laid out
     int read_ctl();
     int ensure_readout(size_t n);
     void drop_graph();
@@ -99,6 +100,9 @@ private:
     bool own_stream_ = false;
 
     std::vector<CircuitPlan> plans_;
+    std::vector<uint32_t> nqs_;                  // the prepared circuits, kept for re-planning
+    std::vector<std::vector<sqc_gate>> gates_;
+    uint32_t max_nx_ = 2;                        // qubits >= 4 a pass may pair across: 1 (pair units) or 2 (quads)
     std::vector<unsigned long long> nb_;
 
     unsigned char* pool_ = nullptr;

@@ -49,7 +49,8 @@ void sqc_batch_default_options(sqc_batch_options* opt) {
     opt->memory_budget = 0;
     opt->use_graph = 0;
     opt->idle_limit_us = 0;
-    for (int i = 0; i < 4; ++i) opt->reserved[i] = 0;
+    opt->threads_per_unit = 0;
+    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_batch_create(const sqc_batch_options* opt, sqc_batch** out) {

@@ -67,13 +67,14 @@ class BatchOptions(ctypes.Structure):
                 ("prune_threshold", ctypes.c_double), ("load_factor", ctypes.c_double),
                 ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
                 ("memory_budget", ctypes.c_uint64), ("use_graph", ctypes.c_uint32),
-                ("idle_limit_us", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
+                ("idle_limit_us", ctypes.c_uint32), ("threads_per_unit", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
 
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("load_factor", ctypes.c_double), ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
                 ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double), ("candidates", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("threads_per_unit", ctypes.c_uint32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -471,7 +472,7 @@ class Batch:
     """
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, min_chunk=8, blocks_per_sm=0,
-                 memory_budget=0, use_graph=False, stream=None, device=0, idle_limit_us=0):
+                 memory_budget=0, use_graph=False, stream=None, device=0, idle_limit_us=0, threads_per_unit=0):
         self._L = load()
         o = BatchOptions()
         self._L.sqc_batch_default_options(ctypes.byref(o))
@@ -485,6 +486,7 @@ class Batch:
         o.stream = stream
         o.device = device
         o.idle_limit_us = idle_limit_us
+        o.threads_per_unit = threads_per_unit
         h = ctypes.c_void_p()
         rc = self._L.sqc_batch_create(ctypes.byref(o), ctypes.byref(h))
         if rc != OK:

@@ -133,8 +133,28 @@ def test_batch_autotune_keeps_results():
     t = b.autotune()
     assert t["candidates"] > 1 and t["best_ms"] > 0 and t["best_ms"] <= t["default_ms"]
     assert t["min_chunk"] in (4, 8, 16, 32) and t["load_factor"] in (0.45, 0.25)
+    assert t["threads_per_unit"] in (16, 32)
     after = [b.state(i) for i in range(len(cs))]
     assert all(_same(x, y) for x, y in zip(before, after))
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_batch_threads_per_unit_keeps_results(precision):
+    """Pair units on half-warps (16 threads, one qubit >= 4 per pass) and quad units on whole
+    warps (32 threads, two per pass) give the same bits, and those of each circuit alone."""
+    cs = _mixed(10, 7)
+    out = {}
+    for tpu in (16, 32):
+        b = Batch(precision=precision, threads_per_unit=tpu)
+        b.prepare(cs)
+        b.run()
+        b.sync()
+        out[tpu] = ([b.state(i) for i in range(len(cs))], b.stats()["passes"])
+        b.close()
+    assert all(_same(x, y) for x, y in zip(out[16][0], out[32][0]))
+    assert out[16][1] > out[32][1]
+    for i, (nq, g) in enumerate(cs):
+        assert _same(out[16][0][i], _alone(nq, g, precision))
 
 
 def test_batch_edge_circuits():
