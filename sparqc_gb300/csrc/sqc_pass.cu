@@ -263,21 +263,18 @@ __global__ void __launch_bounds__(kThreads) tiny_kernel(PassArgs a, const TinyPa
 constexpr int kResolveThreads = 256;
 
 // ---- resolve: the owned units of a pass that pairs groups, before the pass -----------------
-// Two phases per chunk of kResolveEntries * kResolveThreads list entries:
-//  * ownership: every thread takes kResolveEntries entries and looks up each unit's members of
-//    smaller index (an entry owns its unit iff none is live; usually one lookup settles it). The
-//    lookups of a thread's entries advance in lockstep, one probe each per step, so their
-//    header loads are in flight together. Each block reserves room for its owned units with one
-//    atomic on ctl->units_n and places them densely, in no particular order;
+// Two phases per chunk of kResolveThreads list entries:
+//  * ownership: every thread takes one entry and looks up the unit's members of smaller index
+//    (the entry owns its unit iff none is live; usually one lookup settles it). Each block
+//    reserves room for its owned units with one atomic on ctl->units_n and places them
+//    densely, in no particular order;
 //  * members: the owners' remaining lookups are spread over the warp's lanes, K = 2^nx lanes
 //    per owner (lane k looks up member k), 32 / K owners at a time, so an owner's members are
 //    found in one round trip rather than one after another.
 // The staged pass deals the units out evenly.
-constexpr int kResolveEntries = 2;
-
 template <int NX>
 __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
-    constexpr int K = 1 << NX, R = kResolveEntries;
+    constexpr int K = 1 << NX;
     __shared__ unsigned warp_at[kResolveThreads / 32];
     __shared__ unsigned long long base_sh;
     Ctl* ctl = a.ctl;
@@ -296,70 +293,23 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
     };
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    constexpr unsigned long long kChunk = (unsigned long long)R * kResolveThreads;
-    for (unsigned long long c0 = (unsigned long long)blockIdx.x * kChunk; c0 < n;
-         c0 += (unsigned long long)gridDim.x * kChunk) {
-        unsigned b[R];
-        int idx[R], k[R];
-        unsigned long long G0[R], pos[R];
-        uint32_t probes[R];
-        bool own[R], act[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const unsigned long long e = c0 + (unsigned long long)r * kResolveThreads + threadIdx.x;
-            b[r] = e < n ? t.list[e] : kNoBucket;
+    for (unsigned long long c0 = (unsigned long long)blockIdx.x * kResolveThreads; c0 < n;
+         c0 += (unsigned long long)gridDim.x * kResolveThreads) {
+        const unsigned long long e = c0 + threadIdx.x;
+        bool own = false;
+        unsigned b = kNoBucket;
+        int idx = 0;
+        unsigned long long G0 = 0;
+        if (e < n) {
+            b = t.list[e];
+            const unsigned long long G = load_hdr(t.hdr + b).group;
+            idx = ((G & m1) ? 1 : 0) | ((NX >= 2 && (G & m2)) ? 2 : 0) | ((NX == 3 && (G & m3)) ? 4 : 0);
+            G0 = G & ~(m1 | m2 | m3);
+            own = true;
+            for (int k = 0; k < idx && own; ++k) own = lookup_group(t, ep, member(G0, k)) < 0;
         }
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            own[r] = false;
-            idx[r] = 0;
-            G0[r] = 0;
-            if (b[r] != kNoBucket) {
-                const unsigned long long G = load_hdr(t.hdr + b[r]).group;
-                idx[r] = ((G & m1) ? 1 : 0) | ((NX >= 2 && (G & m2)) ? 2 : 0) | ((NX == 3 && (G & m3)) ? 4 : 0);
-                G0[r] = G & ~(m1 | m2 | m3);
-                own[r] = true;
-            }
-            k[r] = 0;
-            probes[r] = 0;
-            act[r] = own[r] && idx[r] > 0;
-            pos[r] = mix64(G0[r]) & t.mask;   // member 0
-        }
-        // lookups of the members below each entry's index, one probe per entry per step, with
-        // lookup_group's rule: a non-live bucket or kMaxProbe probes without the group = absent
-        bool any = false;
-#pragma unroll
-        for (int r = 0; r < R; ++r) any = any || act[r];
-        while (any) {
-            any = false;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                if (!act[r]) continue;
-                const Header h = load_hdr_cg(t.hdr + pos[r]);
-                ++probes[r];
-                if (h.epoch != ep || (h.group != member(G0[r], k[r]) && probes[r] >= kMaxProbe)) {
-                    if (++k[r] == idx[r]) {
-                        act[r] = false;   // no member of smaller index is live: the entry owns its unit
-                    } else {
-                        pos[r] = mix64(member(G0[r], k[r])) & t.mask;
-                        probes[r] = 0;
-                    }
-                } else if (h.group == member(G0[r], k[r])) {
-                    own[r] = false;       // a member of smaller index is live and owns the unit
-                    act[r] = false;
-                } else {
-                    pos[r] = (pos[r] + 1) & t.mask;
-                }
-                any = any || act[r];
-            }
-        }
-        unsigned bal[R], cnt = 0;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            bal[r] = __ballot_sync(kFull, own[r]);
-            cnt += __popc(bal[r]);
-        }
-        if (lane == 0) warp_at[w] = cnt;
+        const unsigned bal = __ballot_sync(kFull, own);
+        if (lane == 0) warp_at[w] = __popc(bal);
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned tot = 0;
@@ -371,34 +321,29 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
             base_sh = tot ? atomicAdd(&ctl->units_n, (unsigned long long)tot) : 0ULL;
         }
         __syncthreads();
-        unsigned long long base = base_sh + warp_at[w];
+        const unsigned long long pos = base_sh + warp_at[w] + __popc(bal & ((1u << lane) - 1u));
+        // members of this warp's owners, 32 / K owners per round, lane r * K + k on member k
+        unsigned rem = bal;
+        while (rem) {
+            int src = -1;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const unsigned long long upos = base + __popc(bal[r] & ((1u << lane) - 1u));
-            // members of this warp's owners, 32 / K owners per round, lane q * K + kk on member kk
-            unsigned rem = bal[r];
-            while (rem) {
-                int src = -1;
-#pragma unroll
-                for (int q = 0; q < 32 / K; ++q) {
-                    const int o = rem ? __ffs(rem) - 1 : -1;
-                    if (rem) rem &= rem - 1;
-                    if (q == lane / K) src = o;
-                }
-                const int kk = lane % K;
-                const unsigned long long sG0 = shfl64(G0[r], src < 0 ? 0 : src);
-                const int sidx = __shfl_sync(kFull, idx[r], src < 0 ? 0 : src);
-                const unsigned sb = __shfl_sync(kFull, b[r], src < 0 ? 0 : src);
-                const unsigned long long spos = shfl64(upos, src < 0 ? 0 : src);
-                if (src >= 0) {
-                    // members below the owner's index are absent (that is what made it the owner)
-                    const long long mb = kk == sidx ? (long long)sb : kk < sidx ? -1LL : lookup_group(t, ep, member(sG0, kk));
-                    Unit* u = t.units + spos;
-                    u->b[kk] = mb < 0 ? kNoBucket : (unsigned)mb;
-                    if (kk == 0) u->G0 = sG0;
-                }
+            for (int r = 0; r < 32 / K; ++r) {
+                const int o = rem ? __ffs(rem) - 1 : -1;
+                if (rem) rem &= rem - 1;
+                if (r == lane / K) src = o;
             }
-            base += __popc(bal[r]);
+            const int k = lane % K;
+            const unsigned long long sG0 = shfl64(G0, src < 0 ? 0 : src);
+            const int sidx = __shfl_sync(kFull, idx, src < 0 ? 0 : src);
+            const unsigned sb = __shfl_sync(kFull, b, src < 0 ? 0 : src);
+            const unsigned long long spos = shfl64(pos, src < 0 ? 0 : src);
+            if (src >= 0) {
+                // members below the owner's index are absent (that is what made it the owner)
+                const long long mb = k == sidx ? (long long)sb : k < sidx ? -1LL : lookup_group(t, ep, member(sG0, k));
+                Unit* u = t.units + spos;
+                u->b[k] = mb < 0 ? kNoBucket : (unsigned)mb;
+                if (k == 0) u->G0 = sG0;
+            }
         }
         __syncthreads();   // warp_at and base_sh are reused by the next chunk
     }
@@ -742,7 +687,7 @@ int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int s
     }
     int launched = 0;
     if (nx) {
-        const unsigned long long chunks = list_hint / ((unsigned long long)kResolveEntries * kResolveThreads) + 1;
+        const unsigned long long chunks = list_hint / kResolveThreads + 1;
         const int g = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(chunks, (unsigned long long)sms * 8));
         if (nx == 1) resolve_kernel<1><<<g, kResolveThreads, 0, st>>>(a);
         else if (nx == 2) resolve_kernel<2><<<g, kResolveThreads, 0, st>>>(a);
