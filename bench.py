@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--no-fp32", action="store_true", help="c1-c3 FP64: skip the FP32 run of the same circuit")
     ap.add_argument("--no-extras", action="store_true",
-                    help="default line: skip the batching and serving summaries (keys c4, c5)")
+                    help="default line: skip the summaries of the other configurations (keys c1, c2, c4, c5)")
     ap.add_argument("--circuits", type=int, default=256, help="c4: circuits per batch")
     ap.add_argument("--autotune", action="store_true", help="c4: autotune the batch before timing")
     ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
@@ -485,6 +485,8 @@ def run_gpu(args):
     extras = {}
     if not args.no_extras and world == 1 and args.workload == "c3" and args.k is None and args.gates is None:
         from sparqc_gb300 import circuits as circ
+        extras["c1"] = single_summary(engine, "c1", stream, args.steps, flush)
+        extras["c2"] = single_summary(engine, "c2", stream, args.steps, flush)
         extras["c4"] = batch_summary(engine, circ, stream, args.steps, flush)
         extras["c5"] = serve_summary(engine, circ, stream)
 
@@ -662,6 +664,33 @@ def run_batch(args):
            "passes_per_step": s1["passes"], "table_bytes": s1["table_bytes"]}
     print(json.dumps(out), flush=True)
     b.close()
+
+
+def single_summary(engine, name, stream, steps, flush, precision=64):
+    """Another single-circuit configuration (c1 or c2), timed like the headline, for the default
+    line: amp-updates/s and ms per circuit from CUDA events, L2 flushed before every step."""
+    import torch
+    nq, gates, p = workload(name, 0)
+    s = engine.State(nq, precision=precision, stream=stream.cuda_stream, initial_buckets=1 << max(6, p["k"] - 4 + 1))
+    for _ in range(3):
+        s.set_zero()
+        s.apply(gates)
+        s.sync()
+    upd = s.stats()["amp_updates"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        s.set_zero()
+        s.apply(gates)
+        s.flush()
+        ev[i][1].record(stream)
+    s.sync()
+    ms = sum(x.elapsed_time(y) for x, y in ev) / steps
+    s.close()
+    return {"workload": config_dict(name, p, precision, 1)["workload"], "value": upd / (ms / 1e3),
+            "unit": "amp-updates/s", "ms_per_step": ms}
 
 
 def batch_summary(engine, circuits, stream, steps, flush):
