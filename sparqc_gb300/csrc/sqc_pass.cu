@@ -90,16 +90,16 @@ __device__ __forceinline__ bool could_overflow(const PassArgs& a, unsigned long 
 
 // Blocks per SM the direct kernel's registers are sized for: FP32 fits four without spills,
 // FP64 three.
-// FP64 passes read their gates from shared memory (staged once per block; measured 2-3% faster
-// on large tables), FP32 passes through L1 (the staging's registers cost FP32 more than it
-// saves). Blocks per SM the staged kernel's registers are sized for: FP64 six; FP32 left to the
-// compiler (0: no minimum).
+// Passes read their gates from shared memory, staged once per block (FP64: 2-3% faster on large
+// tables; FP32 staged passes 0.6% on the 64-qubit workload since the per-slot bucket index
+// became 32 bits: before, the staging's registers cost FP32 more than it saved). Blocks per SM
+// the staged kernel's registers are sized for: FP64 six; FP32 left to the compiler (0: no
+// minimum; seven measured no better).
 template <class T, int NX> struct StagedOcc {
     static constexpr int kMin = sizeof(T) == 8 ? (NX == 3 ? 4 : 6) : 0;   // FP64 octets: 53 KB rings, four blocks
 };
-template <class T> struct StageGates { static constexpr bool kOn = sizeof(T) == 8; };
-// The direct kernel's FP32 octet passes also gain from it (1.7% on the 40-qubit workload); the
-// staged kernel's lose (3.5%).
+template <class T> struct StageGates { static constexpr bool kOn = true; };
+// The direct kernel's FP32 octet passes gain from it too (1.7% on the 40-qubit workload).
 template <class T, int NX> struct DirectStage { static constexpr bool kOn = sizeof(T) == 8 || NX == 3; };
 
 // Octet passes (three cross-group qubits) hold four slots per lane: FP64 two blocks, FP32 three.
