@@ -247,7 +247,7 @@ def pass_roofline(s0, s1, alg_step, alg_pair_step, steps, dev_ms, peak, measured
     n_all = (s1["passes"] - s0["passes"]) / steps
     staged = s1["buckets"] > (1 << 20)
     T = "double" if precision == 64 else "float"
-    nx = "1|2|3"   # passes pair across up to three high qubits (octets: FP32, and FP64 on large tables)
+    nx = "1|2|3" if precision == 32 else "1|2"   # FP32 passes pair across up to three high qubits
     kinds = {
         "pair": {"kernel": (f"resolve_kernel<{nx}> + staged_kernel<{T}, {nx}>" if staged
                             else f"direct_kernel<{T}, {nx}>") + " (passes pairing 16-key groups)",

@@ -95,9 +95,8 @@ typedef struct sqc_options {
                                   overlapping one's launch with the other's drain, and cost ~4-9%
                                   of a many-pass circuit. 0 (default): no events */
     uint32_t max_cross_qubits; /* qubits >= 4 one pass may pair keys across (branching or swap gates on
-                                  them), 1, 2 or 3; 0 = default (3 for FP32; for FP64 2 while the
-                                  table has at most 2^20 buckets, 3 above). Results do not depend
-                                  on it. */
+                                  them), 1, 2 or 3; 0 = default (3 for FP32, 2 for FP64). Results do
+                                  not depend on it. */
     uint32_t device_updates_only; /* 1: sqc_stats.amp_updates counts only gates the device applied;
                                   0 (default): gates the host resolved without touching the state
                                   (a known-zero control, an uncontrolled X as a relabelling of the

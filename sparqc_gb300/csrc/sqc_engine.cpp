@@ -96,12 +96,11 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     lf_ = o.load_factor;
     max_run_ = o.max_fused_gates ? std::min<uint32_t>(o.max_fused_gates, kMaxRun) : kMaxRun;
     if (o.max_cross_qubits > 3) return fail(SQC_ERR_ARG, "max_cross_qubits must be 0, 1, 2 or 3");
-    // default (0): three for FP32 (octet passes measured 14% faster on the 40-qubit workload);
-    // for FP64 two while the table takes direct passes and three once it takes staged ones
-    // (flush picks): octet passes hold four slots per lane, which halves the FP64 kernels'
-    // occupancy: the direct kernel ran 10% slower on the 40-qubit workload, while the staged
-    // kernel's fewer passes made the 64-qubit workload 1.4% faster
-    max_nx_ = o.max_cross_qubits;
+    // default: three for FP32 (octet passes measured 14% faster on the 40-qubit workload), two
+    // for FP64 (octet passes hold four slots per lane, which halves the FP64 kernels' occupancy:
+    // the direct kernel ran 10% slower on the 40-qubit workload; on the 64-qubit workload the
+    // staged kernel gained 1.4% from the fewer passes, with 36% fewer bytes moved per circuit)
+    max_nx_ = o.max_cross_qubits ? o.max_cross_qubits : (o.precision == SQC_FP32 ? 3 : 2);
     time_passes_ = o.time_passes != 0;
     dev_upd_only_ = o.device_updates_only != 0;
     device_ = (int)o.device;
@@ -365,8 +364,7 @@ int Engine::flush(bool hold_last) {
         bool fixed;
     };
     std::vector<Span> spans;
-    const uint32_t max_nx = max_nx_ ? max_nx_ : (!dbl_ || !direct_table(tab_.nb) ? 3u : 2u);
-    split_passes(hd, nd, max_run_, max_nx,
+    split_passes(hd, nd, max_run_, max_nx_,
                  [&](size_t g0, size_t g1, uint32_t nx, uint32_t q1, uint32_t q2, uint32_t q3, bool fixed) {
                      spans.push_back(Span{g0, g1, nx, q1, q2, q3, fixed});
                      encode_pass(hd, g0, g1, q1, q3);

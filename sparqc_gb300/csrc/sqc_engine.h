@@ -113,7 +113,7 @@ private:
     bool dev_upd_only_ = false;     // amp updates count device-applied gates only
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
-    uint32_t max_nx_ = 0;        // cross-group qubits per pass at most; 0: by precision and table size
+    uint32_t max_nx_ = 2;        // cross-group qubits per pass at most
     size_t budget_ = 0;
     cudaStream_t stream_ = nullptr;
     bool own_stream_ = false;

@@ -16,8 +16,6 @@ namespace sqc {
 int launch_pass(const PassArgs& a, unsigned long long list_hint, bool dbl, int sms, cudaStream_t st);
 // Tables small enough for tiny_kernel: every pass of a flush in one single-block launch.
 bool tiny_table(unsigned long long buckets);
-// Tables small enough for direct passes (larger ones take resolve + staged passes).
-bool direct_table(unsigned long long buckets);
 // The passes (device array of np records; a's per-pass fields are ignored) in one launch.
 int launch_tiny(const PassArgs& a, const TinyPass* passes, uint32_t np, bool dbl, cudaStream_t st);
 cudaError_t launch_set_zero(const TableDev& t, Ctl* ctl, bool dbl, cudaStream_t st);

@@ -653,7 +653,6 @@ cudaError_t launch_staged(const PassArgs& a, int grid, cudaStream_t st) {
 }  // namespace
 
 bool tiny_table(unsigned long long buckets) { return buckets <= kTinyMaxBuckets; }
-bool direct_table(unsigned long long buckets) { return buckets <= kDirectMaxBuckets; }
 
 int launch_tiny(const PassArgs& a, const TinyPass* passes, uint32_t np, bool dbl, cudaStream_t st) {
     if (a.t.mask + 1 > kTinyMaxBuckets) return -1;
