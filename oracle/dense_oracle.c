@@ -29,12 +29,46 @@ typedef struct {
     int nq, P;            /* qubits; log2 amplitudes per page */
     uint64_t npages;
     double** pages;       /* page i holds amplitudes [i << P, (i + 1) << P) as (re, im) pairs */
+    uint64_t* live;       /* indices of the allocated pages, in no particular order */
+    uint64_t nlive, cap_live;
     int nthreads;
 } dno_state;
 
+/* The page directory of a 40-qubit register has 2^26 entries: gates walk the list of allocated
+ * pages, never the directory. */
 static double* page_alloc(dno_state* st, uint64_t p) {
-    if (!st->pages[p]) st->pages[p] = (double*)calloc((size_t)2 << st->P, sizeof(double));
+    if (st->pages[p]) return st->pages[p];
+    if (st->nlive == st->cap_live) {
+        const uint64_t cap = st->cap_live ? 2 * st->cap_live : 64;
+        uint64_t* l = (uint64_t*)realloc(st->live, cap * sizeof(uint64_t));
+        if (!l) return NULL;
+        st->live = l;
+        st->cap_live = cap;
+    }
+    st->pages[p] = (double*)calloc((size_t)2 << st->P, sizeof(double));
+    if (st->pages[p]) st->live[st->nlive++] = p;
     return st->pages[p];
+}
+
+/* Drop freed pages from the live list. */
+static void live_compact(dno_state* st) {
+    uint64_t n = 0;
+    for (uint64_t i = 0; i < st->nlive; ++i)
+        if (st->pages[st->live[i]]) st->live[n++] = st->live[i];
+    st->nlive = n;
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : x > y;
+}
+
+static void free_pages(dno_state* st) {
+    for (uint64_t i = 0; i < st->nlive; ++i) {
+        free(st->pages[st->live[i]]);
+        st->pages[st->live[i]] = NULL;
+    }
+    st->nlive = 0;
 }
 
 dno_state* dno_create(int nq) {
@@ -46,15 +80,16 @@ dno_state* dno_create(int nq) {
     st->npages = 1ULL << (nq - st->P);
     st->pages = (double**)calloc(st->npages, sizeof(double*));
     st->nthreads = 1;
-    if (!st->pages || !page_alloc(st, 0)) { free(st->pages); free(st); return NULL; }
+    if (!st->pages || !page_alloc(st, 0)) { free(st->pages); free(st->live); free(st); return NULL; }
     st->pages[0][0] = 1.0;
     return st;
 }
 
 void dno_destroy(dno_state* st) {
     if (!st) return;
-    for (uint64_t p = 0; p < st->npages; ++p) free(st->pages[p]);
+    free_pages(st);
     free(st->pages);
+    free(st->live);
     free(st);
 }
 
@@ -62,7 +97,7 @@ void dno_set_threads(dno_state* st, int n) { st->nthreads = n > 0 ? n : 1; }
 
 /* Replace the state by the given entries (keys < 2^nq). Returns -1 on a bad key. */
 int dno_set_state(dno_state* st, const uint64_t* keys, const double* re, const double* im, uint64_t n) {
-    for (uint64_t p = 0; p < st->npages; ++p) { free(st->pages[p]); st->pages[p] = NULL; }
+    free_pages(st);
     for (uint64_t i = 0; i < n; ++i) {
         if (st->nq < 64 && (keys[i] >> st->nq)) return -1;
         double* pg = page_alloc(st, keys[i] >> st->P);
@@ -104,26 +139,31 @@ static int apply_w(dno_state* st, int w, const uint32_t* t, uint64_t controls, c
     const uint64_t in_mask = (1ULL << P) - 1;
     const uint64_t pt_mask = tmask >> P;             /* target bits above the page offset */
     const uint64_t pc_mask = controls >> P, c_in = controls & in_mask;
-    /* allocate every page a live group touches, before the parallel update */
-    for (uint64_t p = 0; p < st->npages; ++p) {
-        if ((p & pt_mask) || (p & pc_mask) != pc_mask) continue;   /* base pages with the page-level bits clear */
-        int live = 0;
+    /* the base pages (page-level target bits clear, page-level controls set) of the groups
+     * that hold an allocated page; then every page of those groups is allocated, before the
+     * parallel update */
+    uint64_t* base = (uint64_t*)malloc((st->nlive ? st->nlive : 1) * sizeof(uint64_t));
+    if (!base) return -2;
+    uint64_t nb = 0;
+    for (uint64_t i = 0; i < st->nlive; ++i) {
+        const uint64_t b = st->live[i] & ~pt_mask;
+        if ((b & pc_mask) == pc_mask) base[nb++] = b;
+    }
+    qsort(base, nb, sizeof(uint64_t), cmp_u64);
+    uint64_t nu = 0;
+    for (uint64_t i = 0; i < nb; ++i)
+        if (!nu || base[nu - 1] != base[i]) base[nu++] = base[i];
+    for (uint64_t i = 0; i < nu; ++i) {
         for (uint64_t s = pt_mask;; s = (s - 1) & pt_mask) {
-            live |= st->pages[p | s] != NULL;
-            if (!s) break;
-        }
-        if (!live) continue;
-        for (uint64_t s = pt_mask;; s = (s - 1) & pt_mask) {
-            if (!page_alloc(st, p | s)) return -2;
+            if (!page_alloc(st, base[i] | s)) { free(base); return -2; }
             if (!s) break;
         }
     }
     const uint64_t in_tmask = tmask & in_mask;
-    const int64_t np = (int64_t)st->npages;
+    const int64_t np = (int64_t)nu;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(st->nthreads)
     for (int64_t pi = 0; pi < np; ++pi) {
-        const uint64_t p = (uint64_t)pi;
-        if ((p & pt_mask) || (p & pc_mask) != pc_mask || !st->pages[p]) continue;
+        const uint64_t p = base[pi];
         for (uint64_t o = 0; o <= in_mask; ++o) {
             if ((o & in_tmask) || (o & c_in) != c_in) continue;
             double vr[16], vi[16], orr[16], oi[16];
@@ -153,6 +193,8 @@ static int apply_w(dno_state* st, int w, const uint32_t* t, uint64_t controls, c
             if (!s) break;
         }
     }
+    free(base);
+    live_compact(st);
     return 0;
 }
 
@@ -169,12 +211,13 @@ int dno_apply2(dno_state* st, uint32_t a, uint32_t b, uint64_t controls, const d
 
 /* Entries with !(|re| < thr && |im| < thr), key-sorted, into caller arrays. Returns the count
  * (entries beyond cap are counted, not written). */
-uint64_t dno_get_state(const dno_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, double thr) {
+uint64_t dno_get_state(dno_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, double thr) {
     uint64_t n = 0;
     const uint64_t per = 1ULL << st->P;
-    for (uint64_t p = 0; p < st->npages; ++p) {
+    qsort(st->live, st->nlive, sizeof(uint64_t), cmp_u64);   /* key order */
+    for (uint64_t i = 0; i < st->nlive; ++i) {
+        const uint64_t p = st->live[i];
         const double* pg = st->pages[p];
-        if (!pg) continue;
         for (uint64_t o = 0; o < per; ++o) {
             const double r = pg[2 * o], i = pg[2 * o + 1];
             const double ar = r < 0 ? -r : r, ai = i < 0 ? -i : i;

@@ -45,15 +45,29 @@ def engine_run(nq, gates, precision, k):
 
 
 def fidelity(a, b):
-    """|<a|b>|^2 / (<a|a><b|b>) and max |a_k - b_k| over the union of keys (absent = 0)."""
-    keys = np.union1d(a[0], b[0])
-    va = np.zeros(keys.size, np.complex128)
-    vb = np.zeros(keys.size, np.complex128)
-    va[np.searchsorted(keys, a[0])] = a[1] + 1j * a[2]
-    vb[np.searchsorted(keys, b[0])] = b[1] + 1j * b[2]
-    ov = np.vdot(vb, va)
-    f = abs(ov) ** 2 / (np.vdot(va, va).real * np.vdot(vb, vb).real)
-    return float(f), float(np.abs(va - vb).max()) if keys.size else 0.0
+    """|<a|b>|^2 / (<a|a><b|b>) and max |a_k - b_k| over the union of keys (absent = 0), for
+    key-sorted states: a binary search pairs the common keys, so no union array is built."""
+    ka, kb = a[0], b[0]
+    if ka.size == 0 or kb.size == 0:
+        return 0.0, float(max(np.hypot(a[1], a[2]).max(initial=0.0), np.hypot(b[1], b[2]).max(initial=0.0)))
+    if ka.size == kb.size and np.array_equal(ka, kb):
+        ia, hit = np.arange(ka.size), np.ones(kb.size, bool)
+        ar, ai, br, bi = a[1], a[2], b[1], b[2]
+    else:
+        ia = np.minimum(np.searchsorted(ka, kb), ka.size - 1)
+        hit = ka[ia] == kb                  # b's keys that a holds, and where
+        ia = ia[hit]
+        ar, ai, br, bi = a[1][ia], a[2][ia], b[1][hit], b[2][hit]
+    ov_r = np.dot(br, ar) + np.dot(bi, ai)  # <b|a> over the common keys
+    ov_i = np.dot(br, ai) - np.dot(bi, ar)
+    na = np.dot(a[1], a[1]) + np.dot(a[2], a[2])
+    nb = np.dot(b[1], b[1]) + np.dot(b[2], b[2])
+    err = np.hypot(ar - br, ai - bi).max(initial=0.0)
+    only_a = np.ones(ka.size, bool)
+    only_a[ia] = False
+    err = max(err, np.hypot(a[1][only_a], a[2][only_a]).max(initial=0.0),
+              np.hypot(b[1][~hit], b[2][~hit]).max(initial=0.0))
+    return float((ov_r * ov_r + ov_i * ov_i) / (na * nb)), float(err)
 
 
 def assert_near_dense(got, want, rel=1e-12, floor=1e-13):
