@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: table memory budget")
     ap.add_argument("--slice-ms", type=float, default=2.0, help="c5: serving time slice")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--schedule", default="auto", choices=["auto", "on", "off"],
+                    help="c4/c5: gates in sqc_schedule_gates order (auto: on in FP32, off in FP64)")
     ap.add_argument("--k", type=int, default=None, help="override the workload's branching-qubit count")
     ap.add_argument("--gates", type=int, default=None, help="override the workload's gate count")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
@@ -287,6 +289,39 @@ def profile_for(args, staged):
     return f"{'staged' if staged else 'direct'}_kernel_{args.workload}_{prec}"
 
 
+def host_numa(device):
+    """The NUMA node of the GPU (from sysfs) and the nodes of the CPUs this process may run on:
+    page-locked buffers land on the node of the thread that allocates them, and a device-to-host
+    copy to a far node crosses the link between the host's sockets."""
+    import torch
+    out = {}
+    try:
+        pr = torch.cuda.get_device_properties(device)
+        bus = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            out["gpu_node"] = int(f.read().strip())
+    except Exception:
+        out["gpu_node"] = None
+    try:
+        cpus = os.sched_getaffinity(0)
+        nodes = set()
+        for d in os.listdir("/sys/devices/system/node"):
+            if d.startswith("node") and d[4:].isdigit():
+                with open(f"/sys/devices/system/node/{d}/cpulist") as f:
+                    txt = f.read().strip()
+                ids = set()
+                for part in txt.split(","):
+                    if part:
+                        a, _, b = part.partition("-")
+                        ids.update(range(int(a), int(b or a) + 1))
+                if ids & cpus:
+                    nodes.add(int(d[4:]))
+        out["cpu_nodes"] = sorted(nodes)
+    except Exception:
+        out["cpu_nodes"] = None
+    return out
+
+
 def pinned(n, dtype):
     """A page-locked host array of n elements (torch's pinned allocator, viewed as numpy)."""
     import torch
@@ -414,18 +449,24 @@ def run_gpu(args):
     gates_c = np.ascontiguousarray(gates)
     e2e_steps = max(3, min(args.steps, 5))
 
+    read_s = [0.0]
+
     def e2e_step():
         st.set_zero()
         st.apply(gates_c)
+        st.sync()
+        t = time.perf_counter()
         rc = L.sqc_get_state(st.handle, keys.ctypes.data_as(engine.ctypes.c_void_p),
                              re.ctypes.data_as(engine.ctypes.c_void_p), im.ctypes.data_as(engine.ctypes.c_void_p),
                              keys.size, engine.ctypes.byref(got), 0)
+        read_s[0] += time.perf_counter() - t
         if rc != 0:
             raise RuntimeError(f"sqc_get_state failed: {rc}")
         return got.value
 
     e2e_step()   # untimed: the first readout sizes the engine's readout buffers
     torch.cuda.synchronize()
+    read_s[0] = 0.0
     t0 = time.perf_counter()
     nout = 0
     for _ in range(e2e_steps):
@@ -433,7 +474,11 @@ def run_gpu(args):
     e2e_t = (time.perf_counter() - t0) / e2e_steps
     e2e = {"value": upd_per_step * world / e2e_t, "unit": "amp-updates/s",
            "h2d_bytes_per_step": int(gates.size * 136), "d2h_bytes_per_step": int(nout * 24),
-           "path": "sqc_set_zero_state + sqc_apply_gates (host gate array) + sqc_get_state (host arrays)"}
+           "ms_per_step": 1e3 * e2e_t, "readout_ms_per_step": 1e3 * read_s[0] / e2e_steps,
+           "readout_gbs": nout * 24 / (read_s[0] / e2e_steps) / 1e9 if read_s[0] > 0 else None,
+           "host_numa": host_numa(local),
+           "path": "sqc_set_zero_state + sqc_apply_gates (host gate array) + sqc_sync + sqc_get_state (host arrays, "
+                   "page-locked)"}
 
     # the kernel durations of the roofline: the same steps again, every pass bracketed by CUDA
     # events (time_passes), on a second state of the same circuit
@@ -457,30 +502,51 @@ def run_gpu(args):
     sd.close()
     fp64_fma_rate = engine.fp64_rate(local)
 
-    # the same circuit with FP32 amplitudes (FP64 norm and prune comparisons), timed the same way,
-    # and its fidelity against the FP64 result of the timed steps
-    fp32 = None
-    if args.precision == 64 and not args.no_fp32:
-        s32 = engine.State(nq, precision=32, stream=stream.cuda_stream, initial_buckets=1 << max(6, p["k"] - 4 + 1))
+    def variant(precision, schedule):
+        """The same circuit on another state (precision, gate order), timed the same way; its
+        fidelity against the FP64 result of the timed steps."""
+        sv = engine.State(nq, precision=precision, stream=stream.cuda_stream,
+                          initial_buckets=1 << max(6, p["k"] - 4 + 1), schedule_gates=schedule)
         for _ in range(max(3, args.warmup)):
-            s32.set_zero()
-            s32.apply(gates)
-            s32.sync()
-        q0 = s32.stats()
-        ev32 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+            sv.set_zero()
+            sv.apply(gates)
+            sv.sync()
+        q0 = sv.stats()
+        evv = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         torch.cuda.synchronize()
-        timed_steps(s32, ev32)
-        s32.sync()
-        q1 = s32.stats()
-        ms32 = sum(a.elapsed_time(b) for a, b in ev32)
-        fid32, err32 = s32.compare(st)
+        timed_steps(sv, evv)
+        sv.sync()
+        q1 = sv.stats()
+        ms = sum(a.elapsed_time(b) for a, b in evv)
+        fid, err = sv.compare(st)
+        sv.close()
+        return q0, ms, (q1["passes"] - q0["passes"]) / args.steps, fid, err
+
+    # the same circuit with FP32 amplitudes (FP64 norm and prune comparisons), in the given order
+    # and in scheduled order (sqc_options.schedule_gates); FP64 in scheduled order, an option that
+    # gives up bit-identity with the reference's order
+    fp32 = sched64 = None
+    if args.precision == 64 and not args.no_fp32:
+        q0, ms32, np32, fid32, err32 = variant(32, False)
+        q32 = q0
         fp32 = {"value": q0["amp_updates"] * args.steps / (ms32 / 1e3), "unit": "amp-updates/s",
                 "ms_per_step": ms32 / args.steps, "dtype": "f32",
                 "whole_step_achieved_gbs": q0["alg_bytes"] * args.steps / (ms32 / 1e3) / 1e9,
                 "whole_step_frac": q0["alg_bytes"] * args.steps / (ms32 / 1e3) / 1e9 / (
                     (measured_peaks() or {}).get("hbm_gbs", 6800.0)),
-                "passes_per_step": (q1["passes"] - q0["passes"]) / args.steps, "fidelity_vs_fp64": fid32, "max_abs_err_vs_fp64": err32}
-        s32.close()
+                "passes_per_step": np32, "fidelity_vs_fp64": fid32, "max_abs_err_vs_fp64": err32}
+        q0, mss, nps, fids, errs = variant(32, True)
+        fp32["amp_updates_per_step"] = q32["amp_updates"]
+        fp32["scheduled"] = {"ms_per_step": mss / args.steps, "passes_per_step": nps, "fidelity_vs_fp64": fids,
+                             "amp_updates_per_step": q0["amp_updates"],
+                             "max_abs_err_vs_fp64": errs,
+                             "order": "sqc_schedule_gates (gates moved ahead of gates they commute with)"}
+        q0, ms6, np6, fid6, err6 = variant(64, True)
+        sched64 = {"ms_per_step": ms6 / args.steps, "passes_per_step": np6, "fidelity_vs_given_order": fid6,
+                   "amp_updates_per_step": q0["amp_updates"],
+                   "max_abs_err_vs_given_order": err6,
+                   "note": "opt-in (sqc_options.schedule_gates): the same state in exact arithmetic, rounded in "
+                           "another order, so not bit-identical to the reference; the headline keeps the given order"}
 
     extras = {}
     if not args.no_extras and world == 1 and args.workload == "c3" and args.k is None and args.gates is None:
@@ -521,7 +587,7 @@ def run_gpu(args):
                                   "per_step": dev_upd_per_step, "all_gates_per_step": upd_per_step,
                                   "note": "gates applied on the device only; `value` also credits the gates the "
                                           "host resolved without touching the state, as the reference runs them"},
-           "fp32": fp32}
+           "fp32": fp32, "fp64_scheduled": sched64}
     out.update(extras)
     print(json.dumps(out), flush=True)
     st.close()
@@ -556,7 +622,8 @@ def run_batch(args):
     cs = [(nq, g) for nq, _, g in circuits.batch_circuits(args.circuits, seed=rank)]
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    b = engine.Batch(precision=args.precision, use_graph=True, stream=stream.cuda_stream)
+    b = engine.Batch(precision=args.precision, use_graph=True, stream=stream.cuda_stream,
+                     schedule_gates=scheduled(args))
     b.prepare(cs)
     tuning = b.autotune() if args.autotune else None
     for _ in range(max(3, args.warmup)):
@@ -647,6 +714,7 @@ def run_batch(args):
            "config": {"workload": f"c4: {len(cs)} circuits, qubits 16-48, k 8-18, depth 100-1000, 0-3 controls, "
                                   f"30/30/40 diag/perm/branch, FP{args.precision}, seed {rank}",
                       "circuits": len(cs), "precision": f"fp{args.precision}",
+                      "gate_order": "scheduled (sqc_schedule_gates)" if scheduled(args) else "given",
                       "l2": "flushed before every step (256 MiB write)", "parallelism": f"replicas x{world}"},
            "circuits_per_s": circ_s,
            "plain_fp64_per_circuit": {"circuits_per_s": len(cs) / plain_t, "amp_updates_per_s": plain_upd / plain_t,
@@ -694,24 +762,31 @@ def single_summary(engine, name, stream, steps, flush, precision=64):
 
 
 def batch_summary(engine, circuits, stream, steps, flush):
-    """The batching configuration (256 circuits, FP32, one persistent launch, graph replay) next to
-    the plain per-circuit FP64 path on the same circuits, for the default line."""
+    """The batching configuration (256 circuits, FP32 in scheduled gate order, one persistent
+    launch, graph replay) next to the plain per-circuit FP64 path on the same circuits, for the
+    default line; the same batch in the given gate order beside it."""
     import torch
     cs = [(nq, g) for nq, _, g in circuits.batch_circuits(256, seed=0)]
-    b = engine.Batch(precision=32, use_graph=True, stream=stream.cuda_stream)
-    b.prepare(cs)
-    for _ in range(3):
-        b.run()
+
+    def timed_batch(schedule):
+        b = engine.Batch(precision=32, use_graph=True, stream=stream.cuda_stream, schedule_gates=schedule)
+        b.prepare(cs)
+        for _ in range(3):
+            b.run()
+            b.sync()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            b.run()
+            ev[i][1].record(stream)
         b.sync()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    torch.cuda.synchronize()
-    for i in range(steps):
-        flush.fill_(i & 0xFF)
-        ev[i][0].record(stream)
-        b.run()
-        ev[i][1].record(stream)
-    b.sync()
-    ms = sum(x.elapsed_time(y) for x, y in ev) / steps
+        return b, sum(x.elapsed_time(y) for x, y in ev) / steps
+
+    b0, ms0 = timed_batch(False)
+    b0.close()
+    b, ms = timed_batch(True)
     b64 = engine.Batch(precision=64, stream=stream.cuda_stream)
     b64.prepare(cs)
     b64.run()
@@ -727,42 +802,57 @@ def batch_summary(engine, circuits, stream, steps, flush):
         st.sync()
         st.close()
     plain_t = time.perf_counter() - t0
-    return {"workload": "c4: 256 circuits, qubits 16-48, k 8-18, depth 100-1000, FP32, one persistent launch",
+    return {"workload": "c4: 256 circuits, qubits 16-48, k 8-18, depth 100-1000, FP32, one persistent launch, "
+                        "gates in scheduled order (sqc_batch_options.schedule_gates)",
             "circuits_per_s": len(cs) / (ms / 1e3), "ms_per_batch": ms,
             "plain_fp64_circuits_per_s": len(cs) / plain_t,
             "speedup_vs_plain_fp64": (len(cs) / (ms / 1e3)) / (len(cs) / plain_t),
-            "fp32_min_fidelity_vs_fp64": min(fids)}
+            "fp32_min_fidelity_vs_fp64": min(fids),
+            "given_order": {"ms_per_batch": ms0, "circuits_per_s": len(cs) / (ms0 / 1e3),
+                            "speedup_vs_plain_fp64": (len(cs) / (ms0 / 1e3)) / (len(cs) / plain_t)}}
 
 
 def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
-    """The serving configuration at one saturating arrival rate, FP32, next to the plain per-circuit
-    FP64 path over the same requests back to back, for the default line."""
+    """The serving configuration at one saturating arrival rate, FP32 in scheduled gate order, next
+    to the plain per-circuit FP64 path over the same requests back to back, for the default line;
+    the same stream served in the given gate order beside it."""
     import torch
     reqs = circuits.serving_stream(requests, rate, seed=0)
-    lat, makespan, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0)
-    lat = np.array(lat)
+    lat0, makespan0, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0, schedule=False)
+    lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0, schedule=True)
+    lat, lat0 = np.array(lat), np.array(lat0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _, nq, _, g in reqs:
-        st = engine.State(nq, stream=stream.cuda_stream)
-        st.apply(g)
-        st.sync()
-        st.close()
+        s = engine.State(nq, stream=stream.cuda_stream)
+        s.apply(g)
+        s.sync()
+        s.close()
     plain_t = time.perf_counter() - t0
-    served = len(reqs) / makespan
+    served, served0, plain = len(reqs) / makespan, len(reqs) / makespan0, len(reqs) / plain_t
     return {"workload": f"c5: {requests} Poisson arrivals at {rate:g}/s of c4 circuits plus 5% large "
-                        "(48 qubits, k=24, 2000 gates), 120 GB budget, 2 ms slices, FP32",
+                        "(48 qubits, k=24, 2000 gates), 120 GB budget, 2 ms slices, FP32, gates in scheduled order "
+                        "(sqc_server_options.schedule_gates)",
             "circuits_per_s": served, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-            "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-            "plain_fp64_circuits_per_s": len(reqs) / plain_t, "speedup_vs_plain_fp64": served / (len(reqs) / plain_t),
-            "large": int(sum(1 for r in reqs if r[2] == 24))}
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "device_busy_s": st["busy_ms"] / 1e3,
+            "makespan_s": makespan,
+            "plain_fp64_circuits_per_s": plain, "speedup_vs_plain_fp64": served / plain,
+            "large": int(sum(1 for r in reqs if r[2] == 24)),
+            "given_order": {"circuits_per_s": served0, "p50_ms": 1e3 * float(np.percentile(lat0, 50)),
+                            "p99_ms": 1e3 * float(np.percentile(lat0, 99)), "speedup_vs_plain_fp64": served0 / plain}}
 
 
 # --------------------------------------------------------------------------------------
 # c5: serving a Poisson arrival stream (sqc_server_*), against the plain per-circuit FP64 path
-def serve_stream(engine, stream, reqs, precision, budget, slice_ms):
+def scheduled(args):
+    """Whether the batch and serving workloads apply gates in sqc_schedule_gates order."""
+    return args.schedule == "on" or (args.schedule == "auto" and args.precision == 32)
+
+
+def serve_stream(engine, stream, reqs, precision, budget, slice_ms, schedule=False):
     """Serve reqs [(arrival_s, nq, k, gates)] in wall-clock time. Returns latencies, makespan, stats."""
-    sv = engine.Server(precision=precision, memory_budget=int(budget), slice_ms=slice_ms, stream=stream)
+    sv = engine.Server(precision=precision, memory_budget=int(budget), slice_ms=slice_ms, stream=stream,
+                       schedule_gates=schedule)
     n = len(reqs)
     ids = {}
     lat = [None] * n
@@ -808,7 +898,8 @@ def run_serve(args):
     sweep = []
     for rate in rates:
         reqs = circuits.serving_stream(args.requests, rate, seed=rank)
-        lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, args.precision, budget, args.slice_ms)
+        lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, args.precision, budget, args.slice_ms,
+                                         schedule=scheduled(args))
         lat = np.array(lat)
         sweep.append({"rate_per_s": rate, "requests": len(reqs), "circuits_per_s": len(reqs) / makespan,
                       "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
@@ -829,7 +920,8 @@ def run_serve(args):
     fid = None
     if args.precision == 32:
         sample = [r for r in reqs if r[1] == 48 and r[2] == 24][:4] + [r for r in reqs if r[2] != 24][:16]
-        sv = engine.Server(precision=32, memory_budget=int(budget), slice_ms=args.slice_ms, stream=stream.cuda_stream)
+        sv = engine.Server(precision=32, memory_budget=int(budget), slice_ms=args.slice_ms, stream=stream.cuda_stream,
+                           schedule_gates=scheduled(args))
         rids = [sv.submit(r[1], r[3]) for r in sample]
         fs, es = [], []
         while len(fs) < len(rids):
@@ -854,7 +946,8 @@ def run_serve(args):
            "config": {"workload": f"c5: Poisson arrivals of c4 circuits plus 5% large (48 qubits, k=24, 2000 gates), "
                                   f"{args.requests} requests per rate, budget {args.budget_gb:g} GB, "
                                   f"slice {args.slice_ms:g} ms, FP{args.precision}",
-                      "rates": rates, "precision": f"fp{args.precision}"},
+                      "rates": rates, "precision": f"fp{args.precision}",
+                      "gate_order": "scheduled (sqc_schedule_gates)" if scheduled(args) else "given"},
            "sweep": sweep,
            "plain_fp64_per_circuit": {"circuits_per_s": len(reqs) / plain_t,
                                       "path": "one sqc_create + sqc_apply_gates + sqc_sync per circuit, FP64, "

@@ -103,7 +103,12 @@ typedef struct sqc_options {
                                   keys, a one-sided diagonal gate on a known-zero bit) count too,
                                   each with the key count it acted on, as in the reference, which
                                   runs every gate on the device */
-    uint32_t reserved;
+    uint32_t schedule_gates;   /* 1: each gate array given to sqc_apply_gates is applied in the order
+                                  sqc_schedule_gates gives it (max_cross_qubits as above): gates move
+                                  ahead of gates they commute with, so passes fuse more of them. The
+                                  state is the same in exact arithmetic; rounding and pruning follow
+                                  the new order, so results are no longer bit-identical to the
+                                  reference's. 0 (default): the order given */
 } sqc_options;
 
 typedef struct sqc_state sqc_state;
@@ -217,6 +222,15 @@ enum { SQC_2Q_UNITARY = 0, SQC_2Q_RZZ = 1, SQC_2Q_ISWAP = 2, SQC_2Q_FSIM = 3, SQ
  * receives the count. For batches, servers and partitioned states, which take gate arrays. */
 int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta, double phi,
                    const double* u, sqc_gate* out, uint64_t cap, uint64_t* n);
+/* An order of a gate array that gate passes fuse better, as a permutation: perm[i] receives the
+ * index of the i-th gate to apply. Gates move ahead only of gates they commute with (disjoint
+ * qubits -- targets and controls -- or both diagonal), so the state is the same in exact
+ * arithmetic; rounding and pruning follow the new order. Passes are built greedily from the
+ * first gate not yet placed, taking gates from the next 256 while the pass keeps at most
+ * max_cross_qubits (1..3) qubits >= 4 that branching or swap gates pair keys across. A function of
+ * the gates alone (deterministic). SQC_ERR_ARG for a gate invalid on nq qubits. No counterpart in
+ * the reference, which applies gates in the order given. */
+int sqc_schedule_gates(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_cross_qubits, uint32_t* perm);
 /* Apply one two-qubit gate to a state (the sequence of sqc_twoq_gates). */
 int sqc_apply_twoq(sqc_state* st, uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta,
                    double phi, const double* u);
@@ -282,7 +296,10 @@ typedef struct sqc_batch_options {
                                   pair of groups per half-warp: one qubit >= 4 per pass) or 32 (a
                                   quad per warp: two qubits >= 4 per pass); 0 = 32. Results do not
                                   depend on it; sqc_batch_autotune picks it */
-    uint32_t reserved[3];
+    uint32_t schedule_gates;   /* 1: each circuit is applied in the order sqc_schedule_gates gives it
+                                  for two cross-group qubits per pass (whatever threads_per_unit),
+                                  as sqc_options.schedule_gates; 0 (default): the order given */
+    uint32_t reserved[2];
 } sqc_batch_options;
 
 /* Tuning picked by sqc_batch_autotune. */
@@ -367,7 +384,10 @@ typedef struct sqc_server_options {
                                   (a placement in the pool, or a large circuit's own tables) fail
                                   as an out-of-memory device would: sqc_server_step returns
                                   SQC_ERR_OOM and the request stays queued; 0 (default) = none */
-    uint32_t reserved[3];
+    uint32_t schedule_gates;   /* 1: each circuit is applied in the order sqc_schedule_gates gives it
+                                  (three cross-group qubits per pass for large FP32 circuits, else
+                                  two), as sqc_options.schedule_gates; 0 (default): the order given */
+    uint32_t reserved[2];
 } sqc_server_options;
 
 enum { SQC_REQ_QUEUED = 0, SQC_REQ_RUNNING = 1, SQC_REQ_DONE = 2 };

@@ -132,6 +132,7 @@ int Batch::init(const sqc_batch_options* opt) {
     if (o.threads_per_unit != 0 && o.threads_per_unit != 16 && o.threads_per_unit != 32)
         return fail(SQC_ERR_ARG, "threads_per_unit must be 0, 16 or 32");
     max_nx_ = o.threads_per_unit == 16 ? 1u : 2u;
+    sched_ = o.schedule_gates != 0;
     use_graph_ = o.use_graph != 0;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
@@ -174,6 +175,14 @@ int Batch::prepare(const sqc_circuit_desc* cs, uint32_t n) {
         if (cs[i].n_gates && !cs[i].gates) return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": null gates");
         nqs[i] = cs[i].nq;
         gates[i].assign(cs[i].gates, cs[i].gates + cs[i].n_gates);
+        if (sched_ && cs[i].n_gates > 1) {   // schedule_gates order for quad passes, whatever the tuning
+            for (uint64_t j = 0; j < cs[i].n_gates; ++j)
+                if (const char* why = check_gate(cs[i].gates[j], cs[i].nq))
+                    return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": " + why);
+            std::vector<uint32_t> perm(cs[i].n_gates);
+            schedule_gates(cs[i].gates, cs[i].n_gates, 2, kMaxRun, kScheduleWindow, perm.data());
+            for (uint64_t j = 0; j < cs[i].n_gates; ++j) gates[i][j] = cs[i].gates[perm[j]];
+        }
     }
     nqs_.swap(nqs);
     gates_.swap(gates);

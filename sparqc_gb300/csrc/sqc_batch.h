@@ -101,7 +101,8 @@ private:
 
     std::vector<CircuitPlan> plans_;
     std::vector<uint32_t> nqs_;                  // the prepared circuits, kept for re-planning
-    std::vector<std::vector<sqc_gate>> gates_;
+    std::vector<std::vector<sqc_gate>> gates_;   // as applied (schedule_gates order when sched_)
+    bool sched_ = false;
     uint32_t max_nx_ = 2;                        // qubits >= 4 a pass may pair across: 1 (pair units) or 2 (quads)
     std::vector<unsigned long long> nb_;
 

@@ -8,6 +8,7 @@
 #include "../../include/sparqc.h"
 #include "sqc_handles.h"
 #include "sqc_kernels.h"
+#include "sqc_plan.h"
 #include "sqc_twoq.h"
 
 namespace {
@@ -53,7 +54,7 @@ void sqc_default_options(sqc_options* opt) {
     opt->time_passes = 0;
     opt->max_cross_qubits = 0;
     opt->device_updates_only = 0;
-    opt->reserved = 0;
+    opt->schedule_gates = 0;
 }
 
 int sqc_create(uint32_t nq, const sqc_hash_table_parameters* params, const sqc_options* opt, sqc_state** out) {
@@ -185,6 +186,16 @@ int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t c
     if (g.size() > cap) return SQC_ERR_CAPACITY;
     if (!g.empty() && !out) return SQC_ERR_ARG;
     for (size_t i = 0; i < g.size(); ++i) out[i] = g[i];
+    return SQC_OK;
+}
+
+int sqc_schedule_gates(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_cross_qubits, uint32_t* perm) {
+    if (nq < 1 || nq > 64 || max_cross_qubits < 1 || max_cross_qubits > 3 || (n && (!gates || !perm)) ||
+        n > 0xFFFFFFFFULL)
+        return SQC_ERR_ARG;
+    for (uint64_t i = 0; i < n; ++i)
+        if (sqc::check_gate(gates[i], nq)) return SQC_ERR_ARG;
+    sqc::schedule_gates(gates, (size_t)n, max_cross_qubits, sqc::kMaxRun, sqc::kScheduleWindow, perm);
     return SQC_OK;
 }
 

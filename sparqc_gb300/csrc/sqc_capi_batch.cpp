@@ -50,7 +50,8 @@ void sqc_batch_default_options(sqc_batch_options* opt) {
     opt->use_graph = 0;
     opt->idle_limit_us = 0;
     opt->threads_per_unit = 0;
-    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
+    opt->schedule_gates = 0;
+    for (int i = 0; i < 2; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_batch_create(const sqc_batch_options* opt, sqc_batch** out) {
@@ -150,7 +151,8 @@ void sqc_server_default_options(sqc_server_options* opt) {
     opt->solo_log2_groups = 0;
     opt->solo_share_pct = 25;
     opt->inject_alloc_failures = 0;
-    for (int i = 0; i < 3; ++i) opt->reserved[i] = 0;
+    opt->schedule_gates = 0;
+    for (int i = 0; i < 2; ++i) opt->reserved[i] = 0;
 }
 
 int sqc_server_create(const sqc_server_options* opt, sqc_server** out) {

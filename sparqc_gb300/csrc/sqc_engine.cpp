@@ -103,6 +103,7 @@ int Engine::init(uint32_t nq, const sqc_hash_table_parameters* params, const sqc
     max_nx_ = o.max_cross_qubits ? o.max_cross_qubits : (o.precision == SQC_FP32 ? 3 : 2);
     time_passes_ = o.time_passes != 0;
     dev_upd_only_ = o.device_updates_only != 0;
+    sched_ = o.schedule_gates != 0;
     device_ = (int)o.device;
 
     int ndev = 0;
@@ -309,7 +310,13 @@ int Engine::apply(const sqc_gate* gates, uint64_t n) {
     for (uint64_t i = 0; i < n; ++i) {
         if (const char* why = check_gate(gates[i], nq_)) return fail(SQC_ERR_ARG, why);
     }
-    pending_.insert(pending_.end(), gates, gates + n);
+    if (sched_ && n > 1) {   // the call's gates in the order passes fuse better (sqc_schedule_gates)
+        perm_.resize(n);
+        schedule_gates(gates, n, max_nx_, max_run_, kScheduleWindow, perm_.data());
+        for (uint64_t i = 0; i < n; ++i) pending_.push_back(gates[perm_[i]]);
+    } else {
+        pending_.insert(pending_.end(), gates, gates + n);
+    }
     if (pending_.size() >= kFlushAt) return flush();
     return SQC_OK;
 }

@@ -111,6 +111,8 @@ private:
     bool dbl_ = true;
     double thr_ = 1e-14;
     bool dev_upd_only_ = false;     // amp updates count device-applied gates only
+    bool sched_ = false;            // each apply() call's gates go in schedule_gates order
+    std::vector<uint32_t> perm_;    // its scratch
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
     uint32_t max_nx_ = 2;        // cross-group qubits per pass at most

@@ -1,8 +1,10 @@
 // Host-side gate planning: see sqc_plan.h.
 #include "sqc_plan.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace sqc {
 
@@ -93,6 +95,50 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3) {
             }
         }
         g.flip = op;
+    }
+}
+
+void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run, size_t window, uint32_t* perm) {
+    // what each gate is, planned in the given order: a move below only passes gates whose
+    // qubits are disjoint from its own (or diagonal gates past diagonal gates), which change
+    // none of the key bits its planning reads, so it plans the same in the new order
+    std::vector<unsigned char> dev(n), cross(n), diag(n), done(n, 0);
+    std::vector<unsigned long long> sup(n);
+    Planner p;
+    for (size_t i = 0; i < n; ++i) {
+        GateDesc d;
+        dev[i] = plan_gate(p, g[i], &d) ? 1 : 0;
+        cross[i] = dev[i] && !streamable(d);
+        diag[i] = is_diag_kind(g[i].kind) ? 1 : 0;
+        sup[i] = (1ULL << g[i].target) | g[i].controls;
+    }
+    size_t out = 0, first = 0;
+    while (first < n) {
+        if (done[first]) {
+            ++first;
+            continue;
+        }
+        uint32_t q[3] = {kNoQubit, kNoQubit, kNoQubit};
+        uint32_t nx = 0;
+        size_t run = 0;
+        unsigned long long left_any = 0, left_nondiag = 0;   // qubits of the gates left behind
+        const size_t end = std::min(n, first + window);
+        for (size_t i = first; i < end && run < max_run; ++i) {
+            if (done[i]) continue;
+            bool take = (sup[i] & (diag[i] ? left_nondiag : left_any)) == 0;
+            const uint32_t t = g[i].target;
+            const bool new_q = cross[i] && t != q[0] && t != q[1] && t != q[2];
+            if (take && new_q && nx >= max_nx) take = false;
+            if (!take) {
+                left_any |= sup[i];
+                if (!diag[i]) left_nondiag |= sup[i];
+                continue;
+            }
+            if (new_q) q[nx++] = t;
+            run += dev[i];
+            done[i] = 1;
+            perm[out++] = (uint32_t)i;
+        }
     }
 }
 

@@ -78,6 +78,16 @@ void split_passes(const GateDesc* d, size_t n, size_t max_run, uint32_t max_nx, 
 // pair lanes (shuffles).
 void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3 = kNoQubit);
 
+// An order of gates g[0..n) that passes fuse better, as a permutation: perm[i] is the index of
+// the i-th gate to apply. Passes are built greedily from the first gate not yet placed: a gate
+// within the next `window` joins the pass when it commutes with every gate it moves ahead of
+// (their qubits -- target and controls -- are disjoint, or both gates are diagonal) and the
+// pass still has room for it (at most max_nx cross-group qubits, max_run device gates).
+// Commuting gates give the same state in either order; rounding and pruning follow the new
+// order. Deterministic: a function of the gates alone.
+void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run, size_t window, uint32_t* perm);
+constexpr size_t kScheduleWindow = 256;
+
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose
 // planning ended in p (starting from keys that agreed on every bit of the starting kmask):
 // 2^(bits >= 4 that have ever differed between keys).

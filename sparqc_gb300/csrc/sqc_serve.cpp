@@ -64,6 +64,7 @@ int Server::init(const sqc_server_options* opt) {
     max_slots_ = o.max_slots;
     slice_ms_ = o.slice_ms;
     inject_fail_ = o.inject_alloc_failures;
+    sched_ = o.schedule_gates != 0;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
     float tf = (float)o.prune_threshold;
@@ -131,8 +132,24 @@ int Server::submit(const sqc_circuit_desc* c, uint64_t* id) {
     if (const char* why = plan_circuit(c->nq, c->gates, c->n_gates, kMaxRun, 2, &r.plan)) return fail(SQC_ERR_ARG, why);
     r.nb = slice_buckets(r.plan.bound, lf_);
     r.solo = r.plan.bound >= solo_min_groups_ && r.nb && solo_bytes(r) <= solo_cap_;
+    // schedule_gates order, for the passes that will run the circuit: the single-state engine's
+    // (three cross-group qubits in FP32, two in FP64) or the pool's quads. The group bound, and
+    // so the placement just decided, does not depend on the order.
+    std::vector<sqc_gate> sched;
+    if (sched_ && c->n_gates > 1) {
+        std::vector<uint32_t> perm(c->n_gates);
+        schedule_gates(c->gates, c->n_gates, r.solo && !dbl_ ? 3u : 2u, kMaxRun, kScheduleWindow, perm.data());
+        sched.resize(c->n_gates);
+        for (uint64_t j = 0; j < c->n_gates; ++j) sched[j] = c->gates[perm[j]];
+        if (!r.solo) {
+            r.plan = CircuitPlan();
+            if (const char* why = plan_circuit(c->nq, sched.data(), sched.size(), kMaxRun, 2, &r.plan))
+                return fail(SQC_ERR_ARG, why);
+        }
+    }
     if (r.solo) {
-        r.gates.assign(c->gates, c->gates + c->n_gates);
+        if (sched.empty()) r.gates.assign(c->gates, c->gates + c->n_gates);
+        else r.gates.swap(sched);
     } else if (!r.nb || request_bytes(r) > alloc_.size()) {
         return fail(SQC_ERR_BUDGET, "the circuit's table slice can never fit the memory budget");
     }

@@ -88,6 +88,7 @@ private:
     unsigned long long solo_min_groups_ = 1ULL << 17;
     size_t solo_cap_ = 0, solo_used_ = 0;
     uint32_t inject_fail_ = 0;   // admissions left to fail on purpose (sqc_server_options.inject_alloc_failures)
+    bool sched_ = false;         // circuits run in schedule_gates order
     std::vector<uint64_t> solo_;         // running solo requests, in admission order
     double prune_thr_ = 1e-14;
     cudaStream_t stream_ = nullptr;

@@ -23,7 +23,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_flush", "sqc_sync", "sqc_nnz", "sqc_get_state", "sqc_norm2", "sqc_compare", "sqc_get_stats",
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
            "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
-           "sqc_load", "sqc_fp64_rate", "sqc_twoq_gates", "sqc_apply_twoq",
+           "sqc_load", "sqc_fp64_rate", "sqc_twoq_gates", "sqc_apply_twoq", "sqc_schedule_gates",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_get_states",
@@ -48,7 +48,7 @@ class Options(ctypes.Structure):
                 ("stream", ctypes.c_void_p), ("device", ctypes.c_uint32),
                 ("max_fused_gates", ctypes.c_uint32), ("time_passes", ctypes.c_uint32),
                 ("max_cross_qubits", ctypes.c_uint32), ("device_updates_only", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("schedule_gates", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -68,7 +68,7 @@ class BatchOptions(ctypes.Structure):
                 ("min_chunk", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
                 ("memory_budget", ctypes.c_uint64), ("use_graph", ctypes.c_uint32),
                 ("idle_limit_us", ctypes.c_uint32), ("threads_per_unit", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("schedule_gates", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class BatchTuning(ctypes.Structure):
@@ -89,7 +89,7 @@ class ServerOptions(ctypes.Structure):
                 ("memory_budget", ctypes.c_uint64), ("max_slots", ctypes.c_uint32), ("min_chunk", ctypes.c_uint32),
                 ("slice_ms", ctypes.c_double), ("solo_log2_groups", ctypes.c_uint32),
                 ("solo_share_pct", ctypes.c_uint32), ("inject_alloc_failures", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("schedule_gates", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class ServerStats(ctypes.Structure):
@@ -262,6 +262,18 @@ def twoq_gates(form, a, b, c=0, controls=0, theta=0.0, phi=0.0, u=None):
     return out[:n.value].copy()
 
 
+def schedule_gates(nq, gates, max_cross_qubits=3):
+    """The order sqc_schedule_gates gives a gate array: a permutation (uint32 indices) that moves
+    gates ahead of gates they commute with, so that passes fuse more gates."""
+    L = load()
+    g = np.ascontiguousarray(gates, GATE_DTYPE)
+    perm = np.zeros(g.size, np.uint32)
+    rc = L.sqc_schedule_gates(nq, _p(g), g.size, max_cross_qubits, _p(perm))
+    if rc != OK:
+        raise SparqcError(rc, f"sqc_schedule_gates: {L.sqc_status_string(rc).decode()}")
+    return perm
+
+
 def fp64_rate(device=0):
     """Measured FP64 fused multiply-add rate of a device (lane operations per second)."""
     L = load()
@@ -277,7 +289,7 @@ class State:
 
     def __init__(self, nq, precision=FP64, prune_threshold=1e-14, load_factor=0.5, initial_buckets=0,
                  stream=None, device=0, max_fused_gates=0, params=None, time_passes=False, max_cross_qubits=0,
-                 device_updates_only=False):
+                 device_updates_only=False, schedule_gates=False):
         self._L = load()
         o = Options()
         self._L.sqc_default_options(ctypes.byref(o))
@@ -291,6 +303,7 @@ class State:
         o.time_passes = 1 if time_passes else 0
         o.max_cross_qubits = max_cross_qubits
         o.device_updates_only = 1 if device_updates_only else 0
+        o.schedule_gates = 1 if schedule_gates else 0
         h = ctypes.c_void_p()
         pp = ctypes.byref(params) if params is not None else None
         rc = self._L.sqc_create(nq, pp, ctypes.byref(o), ctypes.byref(h))
@@ -468,11 +481,13 @@ class Batch:
     """Many independent circuits, each from |0...0>, run by one persistent kernel launch.
 
     ``circuits`` is a list of ``(nq, gates)`` with ``gates`` a GATE_DTYPE array. Each
-    circuit's result is bit-identical to running it alone on a ``State``.
+    circuit's result is bit-identical to running it alone on a ``State`` (with schedule_gates,
+    to running ``gates[schedule_gates(nq, gates, 2)]`` alone).
     """
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, min_chunk=8, blocks_per_sm=0,
-                 memory_budget=0, use_graph=False, stream=None, device=0, idle_limit_us=0, threads_per_unit=0):
+                 memory_budget=0, use_graph=False, stream=None, device=0, idle_limit_us=0, threads_per_unit=0,
+                 schedule_gates=False):
         self._L = load()
         o = BatchOptions()
         self._L.sqc_batch_default_options(ctypes.byref(o))
@@ -487,6 +502,7 @@ class Batch:
         o.device = device
         o.idle_limit_us = idle_limit_us
         o.threads_per_unit = threads_per_unit
+        o.schedule_gates = 1 if schedule_gates else 0
         h = ctypes.c_void_p()
         rc = self._L.sqc_batch_create(ctypes.byref(o), ctypes.byref(h))
         if rc != OK:
@@ -607,7 +623,7 @@ class Server:
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, memory_budget=0, max_slots=1024,
                  min_chunk=8, slice_ms=2.0, stream=None, device=0, solo_log2_groups=0, solo_share_pct=25,
-                 inject_alloc_failures=0):
+                 inject_alloc_failures=0, schedule_gates=False):
         self._L = load()
         o = ServerOptions()
         self._L.sqc_server_default_options(ctypes.byref(o))
@@ -621,6 +637,7 @@ class Server:
         o.solo_log2_groups = solo_log2_groups
         o.solo_share_pct = solo_share_pct
         o.inject_alloc_failures = inject_alloc_failures
+        o.schedule_gates = 1 if schedule_gates else 0
         o.stream = stream
         o.device = device
         h = ctypes.c_void_p()

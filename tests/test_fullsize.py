@@ -5,13 +5,16 @@
   oracle's (the reference's FC algorithm restated on the CPU) bit for bit, and so do the
   amp-update counts.
 * 64-qubit configuration, FP32: bit for bit against the oracle run in FP32, and fidelity
-  |<psi64|psi32>|^2 >= 1 - 1e-6 against the FP64 run (the FP32 amplitudes' own rounding).
+  |<psi64|psi32>|^2 >= 1 - 1e-6 against the FP64 run (the FP32 amplitudes' own rounding); the
+  same with the gates in scheduled order (sqc_schedule_gates), the oracle fed that order.
 * batching configuration (256 circuits, one persistent launch): every member of at most 30
   qubits against the dense FP64 statevector (textbook matrices, no pruning) within
   |a - b| <= 1e-12 |b| + 1e-13 over the union of keys -- the floor covers what the 1e-14 prune
-  discards and gates later mix in; every FP32 member at fidelity >= 1 - 1e-6 against FP64.
-* serving configuration: a Poisson stream with large circuits, served in FP32, each result at
-  fidelity >= 1 - 1e-6 against the plain FP64 per-circuit path.
+  discards and gates later mix in; every FP32 member (scheduled order, as benchmarked) at
+  fidelity >= 1 - 1e-6 against FP64.
+* serving configuration: a Poisson stream with large circuits, served in FP32 in scheduled
+  order (as benchmarked), each result at fidelity >= 1 - 1e-6 against the plain FP64
+  per-circuit path.
 """
 import numpy as np
 import pytest
@@ -19,7 +22,7 @@ import pytest
 from oracle.dense import PagedDenseOracle
 from oracle.sparse import SparseOracle
 from sparqc_gb300 import circuits
-from sparqc_gb300.engine import Batch, Server, State
+from sparqc_gb300.engine import Batch, Server, State, schedule_gates
 from test_oracle import assert_identical
 
 pytestmark = pytest.mark.gpu
@@ -35,8 +38,8 @@ def oracle_run(gates, precision):
     return out
 
 
-def engine_run(nq, gates, precision, k):
-    st = State(nq, precision=precision, initial_buckets=1 << max(6, k - 4 + 1))
+def engine_run(nq, gates, precision, k, schedule=False):
+    st = State(nq, precision=precision, initial_buckets=1 << max(6, k - 4 + 1), schedule_gates=schedule)
     st.apply(gates)
     out = st.state(sorted=True)
     stats = st.stats()
@@ -121,13 +124,26 @@ def test_config3_full_fp32_bitexact_and_fidelity(c3, c3_fp64):
     assert f >= FID and err < 1e-5
 
 
+def test_config3_scheduled_fp32_bitexact_and_fidelity(c3, c3_fp64):
+    # gates in sqc_schedule_gates order (octet passes): the oracle fed that order agrees bit for
+    # bit; against the FP64 run in the given order, the usual FP32 fidelity
+    nq, g = c3
+    got, stats = engine_run(nq, g, 32, 26, schedule=True)
+    want, upd = oracle_run(g[schedule_gates(nq, g, 3)], 32)
+    assert_identical(got, want)
+    assert stats["amp_updates"] == upd
+    f, err = fidelity(got, c3_fp64[0])
+    print(f"64-qubit configuration, scheduled FP32 vs FP64 in order: fidelity 1 - {1 - f:.3e}, max abs err {err:.3e}")
+    assert f >= FID and err < 1e-5
+
+
 def test_config4_members_against_dense_and_fp32_fidelity():
     cs = circuits.batch_circuits(256, seed=0)
     b64 = Batch(precision=64)
     b64.prepare([(nq, g) for nq, _, g in cs])
     b64.run()
     b64.sync()
-    b32 = Batch(precision=32)
+    b32 = Batch(precision=32, schedule_gates=True)   # the batching configuration as benchmarked
     b32.prepare([(nq, g) for nq, _, g in cs])
     b32.run()
     b32.sync()
@@ -153,7 +169,7 @@ def test_config4_members_against_dense_and_fp32_fidelity():
 def test_config5_served_fp32_against_plain_fp64():
     reqs = circuits.serving_stream(48, 1000.0, seed=3, large_fraction=0.1)
     assert any(r[2] == 24 for r in reqs)
-    sv = Server(precision=32, memory_budget=int(120e9), slice_ms=2.0)
+    sv = Server(precision=32, memory_budget=int(120e9), slice_ms=2.0, schedule_gates=True)   # as benchmarked
     rids = {sv.submit(r[1], r[3]): j for j, r in enumerate(reqs)}
     results = {}
     while len(results) < len(reqs):

@@ -115,6 +115,31 @@ int main() {
     CHECK(pool.used() == 0 && pool.largest_free() == (1u << 20));
     CHECK(pool.alloc(2u << 20) == SIZE_MAX);
 
+    // scheduling: H4 H5 H6 H4 H5 with two cross-group qubits per pass takes three passes in
+    // order; H4 and H5 share no qubit with H6 and move ahead of it: two passes
+    {
+        std::vector<sqc_gate> gs = {g(KH, 4), g(KH, 5), g(KH, 6), g(KH, 4), g(KH, 5)};
+        uint32_t perm[5];
+        schedule_gates(gs.data(), gs.size(), 2, 64, 256, perm);
+        const uint32_t want[5] = {0, 1, 3, 4, 2};
+        for (int i = 0; i < 5; ++i) CHECK(perm[i] == want[i]);
+        auto passes = [&](const std::vector<sqc_gate>& v) {
+            Planner q;
+            std::vector<GateDesc> dv;
+            for (const sqc_gate& x : v) { GateDesc y; if (plan_gate(q, x, &y)) dv.push_back(y); }
+            return split(dv, 2).size();
+        };
+        std::vector<sqc_gate> s;
+        for (int i = 0; i < 5; ++i) s.push_back(gs[perm[i]]);
+        CHECK(passes(gs) == 3 && passes(s) == 2);
+        // a gate on a qubit a skipped gate uses stays behind it: Rz(5) after X(5, ctrl 6)
+        std::vector<sqc_gate> h = {g(KH, 4), g(KH, 5), g(KH, 6), g(KX, 5, 1ULL << 6), g(KRZ, 5), g(KRZ, 7)};
+        uint32_t ph[6];
+        schedule_gates(h.data(), h.size(), 2, 64, 256, ph);
+        const uint32_t wh[6] = {0, 1, 5, 2, 3, 4};   // Rz(7) moves up; Rz(5) waits for the X
+        for (int i = 0; i < 6; ++i) CHECK(ph[i] == wh[i]);
+    }
+
     std::printf("fails=%d\n", fails);
     return fails ? 1 : 0;
 }
