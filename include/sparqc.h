@@ -223,13 +223,14 @@ enum { SQC_2Q_UNITARY = 0, SQC_2Q_RZZ = 1, SQC_2Q_ISWAP = 2, SQC_2Q_FSIM = 3, SQ
 int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta, double phi,
                    const double* u, sqc_gate* out, uint64_t cap, uint64_t* n);
 /* An order of a gate array that gate passes fuse better, as a permutation: perm[i] receives the
- * index of the i-th gate to apply. Gates move ahead only of gates they commute with (disjoint
- * qubits -- targets and controls -- or both diagonal), so the state is the same in exact
- * arithmetic; rounding and pruning follow the new order. Passes are built greedily from the
- * first gate not yet placed, taking gates from the next 256 while the pass keeps at most
- * max_cross_qubits (1..3) qubits >= 4 that branching or swap gates pair keys across. A function of
- * the gates alone (deterministic). SQC_ERR_ARG for a gate invalid on nq qubits. No counterpart in
- * the reference, which applies gates in the order given. */
+ * index of the i-th gate to apply. Gates move ahead only of gates they commute with (neither
+ * changes a qubit the other touches: a gate changes its target unless it is diagonal, and only
+ * reads its controls), so the state is the same in exact arithmetic; rounding and pruning follow
+ * the new order. Passes are built greedily from the first gate not yet placed, taking gates from
+ * the next 256 while the pass keeps at most max_cross_qubits (1..3) qubits >= 4 that branching or
+ * swap gates pair keys across; the pass's qubits are the choice, among a few candidates, that
+ * takes the most gates. A function of the gates alone (deterministic). SQC_ERR_ARG for a gate
+ * invalid on nq qubits. No counterpart in the reference, which applies gates in the order given. */
 int sqc_schedule_gates(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_cross_qubits, uint32_t* perm);
 /* Apply one two-qubit gate to a state (the sequence of sqc_twoq_gates). */
 int sqc_apply_twoq(sqc_state* st, uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t controls, double theta,

@@ -98,46 +98,111 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3) {
     }
 }
 
+namespace {
+
+// A gate as the scheduler sees it: its qubits (target and controls), the qubit it changes (its
+// target, unless it is diagonal), and whether the device runs it and pairs keys across groups.
+struct SchedGate {
+    unsigned long long sup, moves;
+    uint32_t target;
+    bool dev, cross;
+};
+
+// One pass built from gate `first` over [first, end): a gate joins when it commutes with every
+// gate left behind so far and fits the pass (cross-group qubits: the nfixed given ones, or with
+// nfixed == 0 the first max_nx used; at most max_run device gates). Two gates commute when
+// neither changes a qubit the other touches: gates act diagonally on their controls, and a
+// diagonal gate on its target too, and operators that are diagonal on their shared qubits and
+// change disjoint ones commute. Appends the gates taken to *took (if given); returns the number
+// of device gates among them.
+size_t sched_pass(const std::vector<SchedGate>& s, const std::vector<unsigned char>& done, size_t first, size_t end,
+                  uint32_t max_nx, size_t max_run, const uint32_t* fixed, uint32_t nfixed, std::vector<uint32_t>* took) {
+    uint32_t q[3] = {kNoQubit, kNoQubit, kNoQubit};
+    uint32_t nx = 0;
+    for (; nx < nfixed; ++nx) q[nx] = fixed[nx];
+    size_t run = 0;
+    unsigned long long left_sup = 0, left_moves = 0;   // of the gates left behind
+    for (size_t i = first; i < end && run < max_run; ++i) {
+        if (done[i]) continue;
+        const SchedGate& x = s[i];
+        bool take = (x.moves & left_sup) == 0 && (x.sup & left_moves) == 0;
+        const bool new_q = x.cross && x.target != q[0] && x.target != q[1] && x.target != q[2];
+        if (take && new_q && (nfixed || nx >= max_nx)) take = false;
+        if (!take) {
+            left_sup |= x.sup;
+            left_moves |= x.moves;
+            continue;
+        }
+        if (new_q) q[nx++] = x.target;
+        run += x.dev ? 1 : 0;
+        if (took) took->push_back((uint32_t)i);
+    }
+    return run;
+}
+
+}  // namespace
+
 void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run, size_t window, uint32_t* perm) {
-    // what each gate is, planned in the given order: a move below only passes gates whose
-    // qubits are disjoint from its own (or diagonal gates past diagonal gates), which change
-    // none of the key bits its planning reads, so it plans the same in the new order
-    std::vector<unsigned char> dev(n), cross(n), diag(n), done(n, 0);
-    std::vector<unsigned long long> sup(n);
+    // what each gate is, planned in the given order: a move below only passes gates that change
+    // none of the key bits the moved gate's planning reads (its target and controls), and the
+    // moved gate changes none of theirs, so every gate plans the same in the new order
+    std::vector<SchedGate> s(n);
+    std::vector<unsigned char> done(n, 0);
     Planner p;
     for (size_t i = 0; i < n; ++i) {
         GateDesc d;
-        dev[i] = plan_gate(p, g[i], &d) ? 1 : 0;
-        cross[i] = dev[i] && !streamable(d);
-        diag[i] = is_diag_kind(g[i].kind) ? 1 : 0;
-        sup[i] = (1ULL << g[i].target) | g[i].controls;
+        SchedGate& x = s[i];
+        x.dev = plan_gate(p, g[i], &d);
+        x.cross = x.dev && !streamable(d);
+        x.target = g[i].target;
+        x.sup = (1ULL << g[i].target) | g[i].controls;
+        x.moves = is_diag_kind(g[i].kind) ? 0ULL : (1ULL << g[i].target);
     }
+    if (max_nx > 3) max_nx = 3;
     size_t out = 0, first = 0;
+    std::vector<uint32_t> took, best;
     while (first < n) {
         if (done[first]) {
             ++first;
             continue;
         }
-        uint32_t q[3] = {kNoQubit, kNoQubit, kNoQubit};
-        uint32_t nx = 0;
-        size_t run = 0;
-        unsigned long long left_any = 0, left_nondiag = 0;   // qubits of the gates left behind
         const size_t end = std::min(n, first + window);
-        for (size_t i = first; i < end && run < max_run; ++i) {
-            if (done[i]) continue;
-            bool take = (sup[i] & (diag[i] ? left_nondiag : left_any)) == 0;
-            const uint32_t t = g[i].target;
-            const bool new_q = cross[i] && t != q[0] && t != q[1] && t != q[2];
-            if (take && new_q && nx >= max_nx) take = false;
-            if (!take) {
-                left_any |= sup[i];
-                if (!diag[i]) left_nondiag |= sup[i];
-                continue;
+        // the pass's cross-group qubits: the first-use choice, or any max_nx of the first
+        // kSchedCandidates qubits the remaining gates pair across, whichever takes the most
+        // device gates (earliest choice on ties)
+        best.clear();
+        size_t best_run = sched_pass(s, done, first, end, max_nx, max_run, nullptr, 0, &best);
+        uint32_t cand[kSchedCandidates];
+        uint32_t m = 0;
+        for (size_t i = first; i < end && m < kSchedCandidates; ++i) {
+            if (done[i] || !s[i].cross) continue;
+            bool seen = false;
+            for (uint32_t c = 0; c < m; ++c) seen = seen || cand[c] == s[i].target;
+            if (!seen) cand[m++] = s[i].target;
+        }
+        const uint32_t k = std::min(max_nx, m);
+        if (k > 0 && m > k) {   // (m == k: the first-use choice already holds them all)
+            uint32_t idx[3] = {0, 1, 2};
+            for (;;) {
+                uint32_t set[3];
+                for (uint32_t a = 0; a < k; ++a) set[a] = cand[idx[a]];
+                const size_t r = sched_pass(s, done, first, end, max_nx, max_run, set, k, nullptr);
+                if (r > best_run) {
+                    best_run = r;
+                    best.clear();
+                    sched_pass(s, done, first, end, max_nx, max_run, set, k, &best);
+                }
+                int a = (int)k - 1;   // next k-subset of [0, m) in lexicographic order
+                while (a >= 0 && idx[a] == m - k + (uint32_t)a) --a;
+                if (a < 0) break;
+                ++idx[a];
+                for (uint32_t b = (uint32_t)a + 1; b < k; ++b) idx[b] = idx[b - 1] + 1;
             }
-            if (new_q) q[nx++] = t;
-            run += dev[i];
+        }
+        if (best.empty()) best.push_back((uint32_t)first);   // (never: the first gate always fits the first-use pass)
+        for (uint32_t i : best) {
             done[i] = 1;
-            perm[out++] = (uint32_t)i;
+            perm[out++] = i;
         }
     }
 }

@@ -81,11 +81,14 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3 = k
 // An order of gates g[0..n) that passes fuse better, as a permutation: perm[i] is the index of
 // the i-th gate to apply. Passes are built greedily from the first gate not yet placed: a gate
 // within the next `window` joins the pass when it commutes with every gate it moves ahead of
-// (their qubits -- target and controls -- are disjoint, or both gates are diagonal) and the
-// pass still has room for it (at most max_nx cross-group qubits, max_run device gates).
-// Commuting gates give the same state in either order; rounding and pruning follow the new
-// order. Deterministic: a function of the gates alone.
+// (neither changes a qubit the other touches: a gate changes its target, unless it is
+// diagonal, and only reads its controls) and the pass still has room for it (at most max_nx
+// cross-group qubits, max_run device gates). The pass's cross-group qubits are the set, among
+// the first-use choice and the max_nx-subsets of the first kSchedCandidates qubits gates pair
+// across, that takes the most device gates. Commuting gates give the same state in either
+// order; rounding and pruning follow the new order. Deterministic: a function of the gates.
 void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run, size_t window, uint32_t* perm);
+constexpr uint32_t kSchedCandidates = 6;
 constexpr size_t kScheduleWindow = 256;
 
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose

@@ -132,12 +132,21 @@ int main() {
         std::vector<sqc_gate> s;
         for (int i = 0; i < 5; ++i) s.push_back(gs[perm[i]]);
         CHECK(passes(gs) == 3 && passes(s) == 2);
-        // a gate on a qubit a skipped gate uses stays behind it: Rz(5) after X(5, ctrl 6)
-        std::vector<sqc_gate> h = {g(KH, 4), g(KH, 5), g(KH, 6), g(KX, 5, 1ULL << 6), g(KRZ, 5), g(KRZ, 7)};
-        uint32_t ph[6];
-        schedule_gates(h.data(), h.size(), 2, 64, 256, ph);
-        const uint32_t wh[6] = {0, 1, 5, 2, 3, 4};   // Rz(7) moves up; Rz(5) waits for the X
-        for (int i = 0; i < 6; ++i) CHECK(ph[i] == wh[i]);
+        // one cross-group qubit per pass: Rz(4) moves ahead of H(5) and Rz(5) (neither changes
+        // a qubit the other touches); Rz(5) stays behind H(5), which changes its qubit
+        std::vector<sqc_gate> h = {g(KH, 4), g(KH, 5), g(KRZ, 5), g(KRZ, 4)};
+        uint32_t ph[4];
+        schedule_gates(h.data(), h.size(), 1, 64, 256, ph);
+        const uint32_t wh[4] = {0, 3, 1, 2};
+        for (int i = 0; i < 4; ++i) CHECK(ph[i] == wh[i]);
+        // the pass's qubits by trial: on (5, 6) the first pass takes H5, H6, CX(6 -> 5), Rz5
+        // and Rz7, none of which touches qubit 4; on the first-use choice (4, 5) it would take
+        // only H4, H5 and Rz7 (H6, left behind, changes the CX's control)
+        std::vector<sqc_gate> k = {g(KH, 4), g(KH, 5), g(KH, 6), g(KX, 5, 1ULL << 6), g(KRZ, 5), g(KRZ, 7)};
+        uint32_t pk[6];
+        schedule_gates(k.data(), k.size(), 2, 64, 256, pk);
+        const uint32_t wk[6] = {1, 2, 3, 4, 5, 0};
+        for (int i = 0; i < 6; ++i) CHECK(pk[i] == wk[i]);
     }
 
     std::printf("fails=%d\n", fails);
