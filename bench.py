@@ -832,7 +832,7 @@ def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
     served, served0, plain = len(reqs) / makespan, len(reqs) / makespan0, len(reqs) / plain_t
     return {"workload": f"c5: {requests} Poisson arrivals at {rate:g}/s of c4 circuits plus 5% large "
                         "(48 qubits, k=24, 2000 gates), 120 GB budget, 2 ms slices, FP32, gates in scheduled order "
-                        "(sqc_server_options.schedule_gates)",
+                        "(sqc_server_options.schedule_gates), overlapped steps (overlap_steps)",
             "circuits_per_s": served, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99)), "device_busy_s": st["busy_ms"] / 1e3,
             "makespan_s": makespan,
@@ -850,9 +850,10 @@ def scheduled(args):
 
 
 def serve_stream(engine, stream, reqs, precision, budget, slice_ms, schedule=False):
-    """Serve reqs [(arrival_s, nq, k, gates)] in wall-clock time. Returns latencies, makespan, stats."""
+    """Serve reqs [(arrival_s, nq, k, gates)] in wall-clock time, steps overlapped with the host's
+    submits and releases (sqc_server_options.overlap_steps). Returns latencies, makespan, stats."""
     sv = engine.Server(precision=precision, memory_budget=int(budget), slice_ms=slice_ms, stream=stream,
-                       schedule_gates=schedule)
+                       schedule_gates=schedule, overlap_steps=True)
     n = len(reqs)
     ids = {}
     lat = [None] * n
@@ -945,7 +946,7 @@ def run_serve(args):
            "vs_baseline": None, "dtype": f"f{args.precision}", "data": "synthetic",
            "config": {"workload": f"c5: Poisson arrivals of c4 circuits plus 5% large (48 qubits, k=24, 2000 gates), "
                                   f"{args.requests} requests per rate, budget {args.budget_gb:g} GB, "
-                                  f"slice {args.slice_ms:g} ms, FP{args.precision}",
+                                  f"slice {args.slice_ms:g} ms, FP{args.precision}, overlapped steps",
                       "rates": rates, "precision": f"fp{args.precision}",
                       "gate_order": "scheduled (sqc_schedule_gates)" if scheduled(args) else "given"},
            "sweep": sweep,

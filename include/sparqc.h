@@ -388,7 +388,12 @@ typedef struct sqc_server_options {
     uint32_t schedule_gates;   /* 1: each circuit is applied in the order sqc_schedule_gates gives it
                                   (three cross-group qubits per pass for large FP32 circuits, else
                                   two), as sqc_options.schedule_gates; 0 (default): the order given */
-    uint32_t reserved[2];
+    uint32_t overlap_steps;    /* 1: sqc_server_step returns once its slice is launched and waits for
+                                  it at the next call, so the caller's work between steps (submits,
+                                  reads, releases) overlaps the device's; a slice's completions are
+                                  reported by the step after it. 0 (default): each step waits for its
+                                  own slice */
+    uint32_t reserved;
 } sqc_server_options;
 
 enum { SQC_REQ_QUEUED = 0, SQC_REQ_RUNNING = 1, SQC_REQ_DONE = 2 };
@@ -399,7 +404,10 @@ typedef struct sqc_server_stats {
     uint64_t steps;                        /* steps that launched work */
     uint64_t kernel_launches;
     uint64_t amp_updates;                  /* of the requests completed so far */
-    uint64_t pool_bytes, pool_used;        /* the memory budget and its part in use */
+    uint64_t pool_bytes, pool_used;        /* the memory budget and its part held by requests (the
+                                              tables of up to four released large circuits are
+                                              kept for the next of the same shape and dropped when
+                                              the room is needed; they are not counted here) */
     double busy_ms;                        /* device time of all steps (CUDA events) */
 } sqc_server_stats;
 
@@ -409,8 +417,9 @@ int sqc_server_destroy(sqc_server* s);
 /* Plan a circuit (from |0...0>) and queue it; *id receives the request id. SQC_ERR_BUDGET if
  * the circuit could never fit the memory budget. */
 int sqc_server_submit(sqc_server* s, const sqc_circuit_desc* circuit, uint64_t* id);
-/* Admit what fits, run one time slice, wait for it. *finished (may be NULL) receives the number
- * of requests that completed during the step. */
+/* Admit what fits, run one time slice, wait for it (with overlap_steps: wait for the previous
+ * step's slice first, then admit and launch this one). *finished (may be NULL) receives the number
+ * of requests whose completion the step found. */
 int sqc_server_step(sqc_server* s, uint32_t* finished);
 /* Ids of completed, unreleased requests (up to cap, oldest first); *n receives their number. */
 int sqc_server_completed(sqc_server* s, uint64_t* ids, uint32_t cap, uint32_t* n);

@@ -152,7 +152,8 @@ void sqc_server_default_options(sqc_server_options* opt) {
     opt->solo_share_pct = 25;
     opt->inject_alloc_failures = 0;
     opt->schedule_gates = 0;
-    for (int i = 0; i < 2; ++i) opt->reserved[i] = 0;
+    opt->overlap_steps = 0;
+    opt->reserved = 0;
 }
 
 int sqc_server_create(const sqc_server_options* opt, sqc_server** out) {

@@ -100,43 +100,54 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3) {
 
 namespace {
 
-// A gate as the scheduler sees it: its qubits (target and controls), the qubit it changes (its
-// target, unless it is diagonal), and whether the device runs it and pairs keys across groups.
-struct SchedGate {
-    unsigned long long sup, moves;
-    uint32_t target;
-    bool dev, cross;
+// The gates of a scheduling window, as the scheduler sees them: the qubits each touches (target
+// and controls), the qubit it changes (its target, unless it is diagonal), its target bit when
+// the device pairs keys across groups for it, and whether the device runs it at all.
+struct SchedWindow {
+    std::vector<unsigned long long> sup, moves, cross;
+    std::vector<unsigned char> dev;
+    std::vector<uint32_t> idx;   // the gates' positions in the input
+    void clear() {
+        sup.clear();
+        moves.clear();
+        cross.clear();
+        dev.clear();
+        idx.clear();
+    }
 };
 
-// One pass built from gate `first` over [first, end): a gate joins when it commutes with every
-// gate left behind so far and fits the pass (cross-group qubits: the nfixed given ones, or with
-// nfixed == 0 the first max_nx used; at most max_run device gates). Two gates commute when
-// neither changes a qubit the other touches: gates act diagonally on their controls, and a
-// diagonal gate on its target too, and operators that are diagonal on their shared qubits and
-// change disjoint ones commute. Appends the gates taken to *took (if given); returns the number
-// of device gates among them.
-size_t sched_pass(const std::vector<SchedGate>& s, const std::vector<unsigned char>& done, size_t first, size_t end,
-                  uint32_t max_nx, size_t max_run, const uint32_t* fixed, uint32_t nfixed, std::vector<uint32_t>* took) {
-    uint32_t q[3] = {kNoQubit, kNoQubit, kNoQubit};
+// One pass over the window's gates (in order, the first one first): a gate joins when it
+// commutes with every gate left behind so far and fits the pass (cross-group qubits: those of
+// fixed_q when nonzero, else the first max_nx used; at most max_run device gates), over the
+// first nscan gates. Two gates commute when neither changes a qubit the other touches: gates
+// act diagonally on their controls, and a diagonal gate on its target too, and operators that
+// are diagonal on their shared qubits and change disjoint ones commute. Appends the positions
+// taken to *took (if given) and returns the number of device gates among them; *limited (if
+// given) tells whether a gate was refused for want of a cross-group qubit.
+size_t sched_pass(const SchedWindow& w, size_t nscan, uint32_t max_nx, size_t max_run, unsigned long long fixed_q,
+                  std::vector<uint32_t>* took, bool* limited) {
+    unsigned long long qmask = fixed_q;
     uint32_t nx = 0;
-    for (; nx < nfixed; ++nx) q[nx] = fixed[nx];
+    const bool fixed = fixed_q != 0;
     size_t run = 0;
+    bool lim = false;
     unsigned long long left_sup = 0, left_moves = 0;   // of the gates left behind
-    for (size_t i = first; i < end && run < max_run; ++i) {
-        if (done[i]) continue;
-        const SchedGate& x = s[i];
-        bool take = (x.moves & left_sup) == 0 && (x.sup & left_moves) == 0;
-        const bool new_q = x.cross && x.target != q[0] && x.target != q[1] && x.target != q[2];
-        if (take && new_q && (nfixed || nx >= max_nx)) take = false;
-        if (!take) {
-            left_sup |= x.sup;
-            left_moves |= x.moves;
-            continue;
-        }
-        if (new_q) q[nx++] = x.target;
-        run += x.dev ? 1 : 0;
-        if (took) took->push_back((uint32_t)i);
+    // written without data-dependent branches: whether a gate joins is close to a coin flip
+    for (size_t r = 0; r < nscan && run < max_run; ++r) {
+        const unsigned long long blocked = (w.moves[r] & left_sup) | (w.sup[r] & left_moves);
+        const unsigned long long new_q = w.cross[r] & ~qmask;
+        const bool refused = (new_q != 0) & (fixed | (nx >= max_nx));
+        const bool take = (blocked == 0) & !refused;
+        lim |= (blocked == 0) & refused;
+        const unsigned long long behind = take ? 0ULL : ~0ULL;
+        left_sup |= w.sup[r] & behind;
+        left_moves |= w.moves[r] & behind;
+        qmask |= new_q & ~behind;
+        nx += (unsigned)(take & (new_q != 0));
+        run += (size_t)(take & (w.dev[r] != 0));
+        if (took && take) took->push_back(w.idx[r]);
     }
+    if (limited) *limited = lim;
     return run;
 }
 
@@ -146,59 +157,73 @@ void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run
     // what each gate is, planned in the given order: a move below only passes gates that change
     // none of the key bits the moved gate's planning reads (its target and controls), and the
     // moved gate changes none of theirs, so every gate plans the same in the new order
-    std::vector<SchedGate> s(n);
-    std::vector<unsigned char> done(n, 0);
+    std::vector<unsigned long long> sup(n), moves(n), cross(n);
+    std::vector<unsigned char> dev(n), done(n, 0);
     Planner p;
     for (size_t i = 0; i < n; ++i) {
         GateDesc d;
-        SchedGate& x = s[i];
-        x.dev = plan_gate(p, g[i], &d);
-        x.cross = x.dev && !streamable(d);
-        x.target = g[i].target;
-        x.sup = (1ULL << g[i].target) | g[i].controls;
-        x.moves = is_diag_kind(g[i].kind) ? 0ULL : (1ULL << g[i].target);
+        const unsigned long long t = 1ULL << g[i].target;
+        dev[i] = plan_gate(p, g[i], &d) ? 1 : 0;
+        cross[i] = dev[i] && !streamable(d) ? t : 0ULL;
+        sup[i] = t | g[i].controls;
+        moves[i] = is_diag_kind(g[i].kind) ? 0ULL : t;
     }
     if (max_nx > 3) max_nx = 3;
     size_t out = 0, first = 0;
-    std::vector<uint32_t> took, best;
+    SchedWindow w;
+    std::vector<uint32_t> best;
     while (first < n) {
         if (done[first]) {
             ++first;
             continue;
         }
-        const size_t end = std::min(n, first + window);
-        // the pass's cross-group qubits: the first-use choice, or any max_nx of the first
-        // kSchedCandidates qubits the remaining gates pair across, whichever takes the most
-        // device gates (earliest choice on ties)
-        best.clear();
-        size_t best_run = sched_pass(s, done, first, end, max_nx, max_run, nullptr, 0, &best);
-        uint32_t cand[kSchedCandidates];
-        uint32_t m = 0;
-        for (size_t i = first; i < end && m < kSchedCandidates; ++i) {
-            if (done[i] || !s[i].cross) continue;
-            bool seen = false;
-            for (uint32_t c = 0; c < m; ++c) seen = seen || cand[c] == s[i].target;
-            if (!seen) cand[m++] = s[i].target;
+        w.clear();   // the window's gates not yet placed
+        for (size_t i = first, end = std::min(n, first + window); i < end; ++i) {
+            if (done[i]) continue;
+            w.sup.push_back(sup[i]);
+            w.moves.push_back(moves[i]);
+            w.cross.push_back(cross[i]);
+            w.dev.push_back(dev[i]);
+            w.idx.push_back((uint32_t)i);
         }
-        const uint32_t k = std::min(max_nx, m);
-        if (k > 0 && m > k) {   // (m == k: the first-use choice already holds them all)
-            uint32_t idx[3] = {0, 1, 2};
-            for (;;) {
-                uint32_t set[3];
-                for (uint32_t a = 0; a < k; ++a) set[a] = cand[idx[a]];
-                const size_t r = sched_pass(s, done, first, end, max_nx, max_run, set, k, nullptr);
-                if (r > best_run) {
-                    best_run = r;
-                    best.clear();
-                    sched_pass(s, done, first, end, max_nx, max_run, set, k, &best);
+        // the pass's cross-group qubits: the first-use choice, or any max_nx of the first
+        // kSchedCandidates qubits the window's gates pair across, whichever takes the most
+        // device gates over the first kSchedTrialWindow gates (earliest choice on ties). A
+        // first-use pass that refused no gate for want of a qubit took every gate it reached (the
+        // first refusal of any other kind needs a gate left behind), so no choice does better.
+        const size_t ntrial = std::min(w.idx.size(), (size_t)kSchedTrialWindow);
+        bool limited = false;
+        size_t best_run = sched_pass(w, ntrial, max_nx, max_run, 0ULL, nullptr, &limited);
+        unsigned long long best_q = 0;
+        if (limited) {
+            unsigned long long cand[kSchedCandidates];
+            uint32_t m = 0;
+            unsigned long long seen = 0;
+            for (size_t r = 0; r < w.idx.size() && m < kSchedCandidates; ++r) {
+                if (w.cross[r] & ~seen) cand[m++] = w.cross[r];
+                seen |= w.cross[r];
+            }
+            const uint32_t k = std::min(max_nx, m);
+            if (k > 0 && m > k) {
+                uint32_t ix[3] = {0, 1, 2};
+                for (;;) {   // every k-subset of the candidates, in lexicographic order
+                    unsigned long long set = 0;
+                    for (uint32_t a = 0; a < k; ++a) set |= cand[ix[a]];
+                    const size_t r = sched_pass(w, ntrial, max_nx, max_run, set, nullptr, nullptr);
+                    if (r > best_run) {   // earliest choice on ties, the first-use one first
+                        best_run = r;
+                        best_q = set;
+                    }
+                    int a = (int)k - 1;
+                    while (a >= 0 && ix[a] == m - k + (uint32_t)a) --a;
+                    if (a < 0) break;
+                    ++ix[a];
+                    for (uint32_t b = (uint32_t)a + 1; b < k; ++b) ix[b] = ix[b - 1] + 1;
                 }
-                int a = (int)k - 1;   // next k-subset of [0, m) in lexicographic order
-                while (a >= 0 && idx[a] == m - k + (uint32_t)a) --a;
-                if (a < 0) break;
-                ++idx[a];
-                for (uint32_t b = (uint32_t)a + 1; b < k; ++b) idx[b] = idx[b - 1] + 1;
             }
         }
+        best.clear();   // the chosen pass over the whole window
+        sched_pass(w, w.idx.size(), max_nx, max_run, best_q, &best, nullptr);
         if (best.empty()) best.push_back((uint32_t)first);   // (never: the first gate always fits the first-use pass)
         for (uint32_t i : best) {
             done[i] = 1;

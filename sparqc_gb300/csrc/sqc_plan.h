@@ -85,10 +85,12 @@ void encode_pass(GateDesc* d, size_t g0, size_t g1, uint32_t q1, uint32_t q3 = k
 // diagonal, and only reads its controls) and the pass still has room for it (at most max_nx
 // cross-group qubits, max_run device gates). The pass's cross-group qubits are the set, among
 // the first-use choice and the max_nx-subsets of the first kSchedCandidates qubits gates pair
-// across, that takes the most device gates. Commuting gates give the same state in either
-// order; rounding and pruning follow the new order. Deterministic: a function of the gates.
+// across, that takes the most device gates over the first kSchedTrialWindow gates of the
+// window. Commuting gates give the same state in either order; rounding and pruning follow the
+// new order. Deterministic: a function of the gates.
 void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run, size_t window, uint32_t* perm);
 constexpr uint32_t kSchedCandidates = 6;
+constexpr uint32_t kSchedTrialWindow = 64;   // gates the candidate choices are compared over
 constexpr size_t kScheduleWindow = 256;
 
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose

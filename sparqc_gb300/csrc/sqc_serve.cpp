@@ -23,9 +23,11 @@ Server::~Server() {
     for (void* p : {(void*)pool_, (void*)d_circ_, (void*)d_ctl_, (void*)d_sched_, (void*)d_words_, (void*)d_cmd_,
                     (void*)d_limit_, (void*)d_bctl_, (void*)d_rk_, (void*)d_rr_, (void*)d_ri_})
         if (p) cudaFree(p);
-    for (void* p : {(void*)h_circ_, (void*)h_ctl_, (void*)h_sched_, (void*)h_cmd_, (void*)h_limit_, (void*)h_bctl_})
+    for (void* p : {(void*)h_circ_, (void*)h_ctl_, (void*)h_sched_, (void*)h_cmd_, (void*)h_limit_, (void*)h_bctl_,
+                    (void*)stg_circ_, (void*)stg_cmd_, (void*)stg_limit_})
         if (p) cudaFreeHost(p);
     reqs_.clear();   // solo engines release their tables before the stream goes
+    spare_.clear();
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev2_) cudaEventDestroy(ev2_);
@@ -65,6 +67,7 @@ int Server::init(const sqc_server_options* opt) {
     slice_ms_ = o.slice_ms;
     inject_fail_ = o.inject_alloc_failures;
     sched_ = o.schedule_gates != 0;
+    overlap_ = o.overlap_steps != 0;
     device_ = (int)o.device;
     std::memcpy(&prune_.d, &o.prune_threshold, sizeof(double));
     float tf = (float)o.prune_threshold;
@@ -104,6 +107,9 @@ int Server::init(const sqc_server_options* opt) {
         (rc = cuda(cudaMallocHost(&h_cmd_, n * sizeof(unsigned)), "cudaMallocHost")) ||
         (rc = cuda(cudaMallocHost(&h_limit_, n * sizeof(unsigned)), "cudaMallocHost")) ||
         (rc = cuda(cudaMallocHost(&h_bctl_, sizeof(BatchCtl)), "cudaMallocHost")) ||
+        (rc = cuda(cudaMallocHost(&stg_circ_, n * sizeof(BCirc)), "cudaMallocHost")) ||
+        (rc = cuda(cudaMallocHost(&stg_cmd_, n * sizeof(unsigned)), "cudaMallocHost")) ||
+        (rc = cuda(cudaMallocHost(&stg_limit_, n * sizeof(unsigned)), "cudaMallocHost")) ||
         (rc = cuda(cudaMemset(d_ctl_, 0, n * sizeof(Ctl)), "cudaMemset")) ||
         (rc = cuda(cudaMemset(d_sched_, 0, n * sizeof(BSched)), "cudaMemset")) ||
         (rc = cuda(cudaMemset(d_words_, 0, n * sizeof(unsigned long long)), "cudaMemset")) ||
@@ -171,6 +177,22 @@ int Server::admit_solo(uint64_t rid, Request& r) {
         --inject_fail_;
         return fail(SQC_ERR_OOM, "injected allocation failure (large circuit's tables)");
     }
+    for (size_t i = 0; i < spare_.size(); ++i) {   // a kept engine of the same shape: reset it
+        if (spare_[i].nq != r.plan.nq || spare_[i].nb != r.nb) continue;
+        std::unique_ptr<Engine> e = std::move(spare_[i].eng);
+        solo_used_ -= spare_[i].bytes;
+        spare_.erase(spare_.begin() + (std::ptrdiff_t)i);
+        const int rc = e->set_zero();
+        if (rc) {
+            err = "solo engine: " + e->err;
+            return rc;
+        }
+        r.eng = std::move(e);
+        solo_used_ += solo_bytes(r);
+        r.state = SQC_REQ_RUNNING;
+        solo_.push_back(rid);
+        return SQC_OK;
+    }
     sqc_options o;
     sqc_default_options(&o);
     o.precision = dbl_ ? SQC_FP64 : SQC_FP32;
@@ -203,7 +225,18 @@ int Server::admit() {
         const uint64_t rid = queue_.front();
         Request& r = reqs_.at(rid);
         if (r.solo) {
-            if (solo_used_ + solo_bytes(r) > solo_cap_) break;
+            // a spare engine of this shape is reused in place; others go when the room is needed
+            size_t reuse = 0;
+            for (const Spare& sp : spare_)
+                if (sp.nq == r.plan.nq && sp.nb == r.nb) reuse = sp.bytes;
+            while (solo_used_ - reuse + solo_bytes(r) > solo_cap_) {
+                size_t k = 0;
+                while (k < spare_.size() && spare_[k].nq == r.plan.nq && spare_[k].nb == r.nb) ++k;
+                if (k == spare_.size()) break;
+                solo_used_ -= spare_[k].bytes;
+                spare_.erase(spare_.begin() + (std::ptrdiff_t)k);   // frees its tables
+            }
+            if (solo_used_ - reuse + solo_bytes(r) > solo_cap_) break;
             if ((rc = admit_solo(rid, r))) return rc;
             queue_.pop_front();
             continue;
@@ -277,6 +310,9 @@ BatchArgs Server::args(uint32_t n) const {
 int Server::step(uint32_t* finished) {
     if (finished) *finished = 0;
     int rc;
+    uint32_t fin = 0;
+    if (in_flight_ && (rc = retire(&fin))) return rc;   // the previous step's slice (overlap_steps)
+    if (finished) *finished = fin;
     if ((rc = admit())) return rc;
     bool any = false;
     for (uint32_t s = 0; s < n_used_ && !any; ++s)
@@ -286,9 +322,12 @@ int Server::step(uint32_t* finished) {
     if ((rc = cuda(cudaEventRecord(ev0_, stream_), "event"))) return rc;
     if (any) {
         // the small circuits: one time slice of the persistent kernel over the resident slots
-        if ((rc = cuda(cudaMemcpyAsync(d_circ_, h_circ_, n * sizeof(BCirc), cudaMemcpyHostToDevice, stream_), "H2D")) ||
-            (rc = cuda(cudaMemcpyAsync(d_cmd_, h_cmd_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "H2D")) ||
-            (rc = cuda(cudaMemcpyAsync(d_limit_, h_limit_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_),
+        std::memcpy(stg_circ_, h_circ_, n * sizeof(BCirc));
+        std::memcpy(stg_cmd_, h_cmd_, n * sizeof(unsigned));
+        std::memcpy(stg_limit_, h_limit_, n * sizeof(unsigned));
+        if ((rc = cuda(cudaMemcpyAsync(d_circ_, stg_circ_, n * sizeof(BCirc), cudaMemcpyHostToDevice, stream_), "H2D")) ||
+            (rc = cuda(cudaMemcpyAsync(d_cmd_, stg_cmd_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_), "H2D")) ||
+            (rc = cuda(cudaMemcpyAsync(d_limit_, stg_limit_, n * sizeof(unsigned), cudaMemcpyHostToDevice, stream_),
                        "H2D")))
             return rc;
         const int grid = sms_ * batch_residency(dbl_, 0);
@@ -314,8 +353,25 @@ int Server::step(uint32_t* finished) {
         // pass goes on fusing the next slice's gates
         if ((rc = r.eng->flush(r.pos + g < r.gates.size()))) { err = r.eng->err; return rc; }
     }
-    if ((rc = cuda(cudaEventRecord(ev2_, stream_), "event")) || (rc = cuda(cudaStreamSynchronize(stream_), "sync")))
-        return rc;
+    if ((rc = cuda(cudaEventRecord(ev2_, stream_), "event"))) return rc;
+    in_flight_ = true;
+    in_any_ = any;
+    in_n_ = n;
+    if (overlap_) return SQC_OK;
+    rc = retire(&fin);
+    if (finished) *finished += fin;
+    return rc;
+}
+
+// Wait for the slice in flight and retire what it finished: solo circuits that applied their
+// last gates, batch slots that ended (parked ones resume at the next launch).
+int Server::retire(uint32_t* finished) {
+    *finished = 0;
+    in_flight_ = false;
+    const bool any = in_any_;
+    const uint32_t n = in_n_;
+    int rc;
+    if ((rc = cuda(cudaStreamSynchronize(stream_), "sync"))) return rc;
     ++steps_;
     float ms = 0.f, ms_solo = 0.f;
     if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) busy_ms_ += ms;
@@ -374,7 +430,7 @@ int Server::step(uint32_t* finished) {
         done_.push_back(rid);
         ++fin;
     }
-    if (finished) *finished = fin;
+    *finished = fin;
     if (timeout) return fail(SQC_ERR_STATE, "serving kernel found no work for too long; running requests failed");
     return SQC_OK;
 }
@@ -493,9 +549,19 @@ int Server::release(uint64_t id) {
     Request& r = it->second;
     if (r.state != SQC_REQ_DONE) return fail(SQC_ERR_STATE, "only completed requests can be released");
     if (r.solo) {
-        solo_used_ -= solo_bytes(r);
+        if (r.eng && r.status == SQC_OK && spare_.size() < kMaxSpare) {
+            // kept for the next large circuit of this shape; its bytes stay counted
+            Spare sp;
+            sp.eng = std::move(r.eng);
+            sp.nq = r.plan.nq;
+            sp.nb = r.nb;
+            sp.bytes = solo_bytes(r);
+            spare_.push_back(std::move(sp));
+        } else {
+            solo_used_ -= solo_bytes(r);
+        }
         done_.erase(std::remove(done_.begin(), done_.end(), id), done_.end());
-        reqs_.erase(it);   // the engine frees its tables
+        reqs_.erase(it);   // an engine not kept frees its tables
         return SQC_OK;
     }
     const int slot = r.slot;
@@ -521,7 +587,9 @@ int Server::stats(sqc_server_stats* out) {
     out->kernel_launches = launches_;
     out->amp_updates = upd_done_;
     out->pool_bytes = alloc_.size() + solo_cap_;
-    out->pool_used = alloc_.used() + solo_used_;
+    size_t spare = 0;   // kept engines are reclaimable, not held by a request
+    for (const Spare& sp : spare_) spare += sp.bytes;
+    out->pool_used = alloc_.used() + solo_used_ - spare;
     out->busy_ms = busy_ms_;
     return SQC_OK;
 }

@@ -4,8 +4,9 @@
 // arrival order while a slot is free and their table slice plus gate descriptors fit the
 // memory pool, then launches the batch kernel over every resident slot with a deadline: new
 // requests start from |0...0>, parked ones resume, and every circuit whose pass ends after the
-// deadline parks again. The step waits for the launch and retires the circuits that finished.
-// Their states stay resident until released.
+// deadline parks again. The step waits for the launch and retires the circuits that finished
+// (with overlap_steps, the next step does, before it admits and launches). Their states stay
+// resident until released.
 #pragma once
 #include <cstdint>
 #include <deque>
@@ -86,9 +87,24 @@ private:
     uint32_t max_slots_ = 1024;
     double slice_ms_ = 2.0;
     unsigned long long solo_min_groups_ = 1ULL << 17;
-    size_t solo_cap_ = 0, solo_used_ = 0;
+    size_t solo_cap_ = 0, solo_used_ = 0;   // solo_used_ includes the spare engines' tables
+    // engines of released large circuits, kept (tables allocated, stream events made) for the
+    // next large circuit of the same qubit count and table size; dropped when the memory is needed
+    struct Spare {
+        std::unique_ptr<Engine> eng;
+        uint32_t nq = 0;
+        unsigned long long nb = 0;
+        size_t bytes = 0;
+    };
+    std::vector<Spare> spare_;
+    static constexpr size_t kMaxSpare = 4;
     uint32_t inject_fail_ = 0;   // admissions left to fail on purpose (sqc_server_options.inject_alloc_failures)
     bool sched_ = false;         // circuits run in schedule_gates order
+    // overlap_steps: a step leaves its slice in flight (in_flight_) and retires it at the next
+    // call; in_any_ and in_n_ describe the slice's batch launch
+    bool overlap_ = false, in_flight_ = false, in_any_ = false;
+    uint32_t in_n_ = 0;
+    int retire(uint32_t* finished);
     std::vector<uint64_t> solo_;         // running solo requests, in admission order
     double prune_thr_ = 1e-14;
     cudaStream_t stream_ = nullptr;
@@ -104,6 +120,9 @@ private:
     unsigned* d_limit_ = nullptr;
     BatchCtl* d_bctl_ = nullptr;
     BCirc* h_circ_ = nullptr;     // pinned mirrors
+    BCirc* stg_circ_ = nullptr;   // what a launch copies to the device, taken from the mirrors at
+    unsigned* stg_cmd_ = nullptr; // launch time so that the host may change them while it runs
+    unsigned* stg_limit_ = nullptr;
     Ctl* h_ctl_ = nullptr;
     BSched* h_sched_ = nullptr;
     unsigned* h_cmd_ = nullptr;

@@ -89,7 +89,7 @@ class ServerOptions(ctypes.Structure):
                 ("memory_budget", ctypes.c_uint64), ("max_slots", ctypes.c_uint32), ("min_chunk", ctypes.c_uint32),
                 ("slice_ms", ctypes.c_double), ("solo_log2_groups", ctypes.c_uint32),
                 ("solo_share_pct", ctypes.c_uint32), ("inject_alloc_failures", ctypes.c_uint32),
-                ("schedule_gates", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("schedule_gates", ctypes.c_uint32), ("overlap_steps", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -623,7 +623,7 @@ class Server:
 
     def __init__(self, precision=FP64, prune_threshold=1e-14, load_factor=0.45, memory_budget=0, max_slots=1024,
                  min_chunk=8, slice_ms=2.0, stream=None, device=0, solo_log2_groups=0, solo_share_pct=25,
-                 inject_alloc_failures=0, schedule_gates=False):
+                 inject_alloc_failures=0, schedule_gates=False, overlap_steps=False):
         self._L = load()
         o = ServerOptions()
         self._L.sqc_server_default_options(ctypes.byref(o))
@@ -638,6 +638,7 @@ class Server:
         o.solo_share_pct = solo_share_pct
         o.inject_alloc_failures = inject_alloc_failures
         o.schedule_gates = 1 if schedule_gates else 0
+        o.overlap_steps = 1 if overlap_steps else 0
         o.stream = stream
         o.device = device
         h = ctypes.c_void_p()

@@ -137,3 +137,22 @@ def test_large_requests_run_alone_with_the_same_result(precision):
         assert _same(got[i], _alone(nq, g, precision)), f"request {i}"
     s = sv.stats()
     assert s["pool_used"] == 0 and s["solo_running"] == 0
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_overlapped_steps_give_the_same_results(precision):
+    # overlap_steps: a step returns with its slice in flight and the next one retires it, so the
+    # submits, reads and releases between steps run while the device works; large circuits run
+    # alone (and their engines are kept for the next of the same shape), small ones in the pool
+    cs = _stream(16, 5)
+    big = [(30, circuits.random_circuit(30, 16, 300, 2, circuits.SplitMix64(950 + i))) for i in range(3)]
+    mix = cs[:5] + big[:1] + cs[5:11] + big[1:] + cs[11:]
+    sv = Server(precision=precision, memory_budget=512 * MB, slice_ms=0.2, solo_log2_groups=6, solo_share_pct=50,
+                overlap_steps=True)
+    got, steps = _serve(sv, mix, per_step=2)
+    assert steps > 5
+    for i, (nq, g) in enumerate(mix):
+        assert _same(got[i], _alone(nq, g, precision)), f"request {i}"
+    s = sv.stats()
+    assert s["pool_used"] == 0 and s["solo_running"] == 0 and s["running"] == 0
+    sv.close()
