@@ -405,7 +405,7 @@ typedef struct sqc_server_stats {
     uint64_t kernel_launches;
     uint64_t amp_updates;                  /* of the requests completed so far */
     uint64_t pool_bytes, pool_used;        /* the memory budget and its part held by requests (the
-                                              tables of up to four released large circuits are
+                                              tables of up to 16 released large circuits are
                                               kept for the next of the same shape and dropped when
                                               the room is needed; they are not counted here) */
     double busy_ms;                        /* device time of all steps (CUDA events) */

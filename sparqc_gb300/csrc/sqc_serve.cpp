@@ -31,6 +31,7 @@ Server::~Server() {
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
     if (ev2_) cudaEventDestroy(ev2_);
+    for (cudaEvent_t e : solo_ev_) cudaEventDestroy(e);
     if (own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -198,7 +199,7 @@ int Server::admit_solo(uint64_t rid, Request& r) {
     o.precision = dbl_ ? SQC_FP64 : SQC_FP32;
     o.prune_threshold = prune_thr_;
     o.initial_buckets = r.nb;
-    o.stream = stream_;
+    o.stream = nullptr;   // its own stream: the large circuits' slices of a step run side by side
     o.device = (uint32_t)device_;
     sqc_hash_table_parameters hp;
     std::memset(&hp, 0, sizeof hp);
@@ -340,18 +341,30 @@ int Server::step(uint32_t* finished) {
         launches_ += 2;
     }
     if ((rc = cuda(cudaEventRecord(ev1_, stream_), "event"))) return rc;
-    // the large circuits: each applies as many of its next gates as fit a time slice at the
-    // rate measured on its previous steps
-    for (uint64_t rid : solo_) {
-        Request& r = reqs_.at(rid);
+    // the large circuits, after the batch slice, side by side on their engines' streams: each
+    // applies as many of its next gates as fit a time slice at the rate the large circuits
+    // together achieved on the previous steps (so a step holds about a slice per large circuit,
+    // as when they ran one after the other); the server's stream then waits for all of them
+    while (solo_ev_.size() < solo_.size()) {
+        cudaEvent_t e;
+        if ((rc = cuda(cudaEventCreate(&e), "event"))) return rc;
+        solo_ev_.push_back(e);
+    }
+    for (size_t k = 0; k < solo_.size(); ++k) {
+        Request& r = reqs_.at(solo_[k]);
+        const cudaStream_t es = r.eng->stream();
         const uint64_t left = r.gates.size() - r.pos;
         uint64_t g = r.ms_per_gate > 0.0 ? (uint64_t)(slice_ms_ / r.ms_per_gate) : 32;
         g = std::min<uint64_t>(std::max<uint64_t>(8, g), left);
         r.chunk = g;
+        if ((rc = cuda(cudaStreamWaitEvent(es, ev1_, 0), "wait"))) return rc;
         if (g && (rc = r.eng->apply(r.gates.data() + r.pos, g))) { err = r.eng->err; return rc; }
         // a slice that does not end the circuit keeps its last, unfinished pass queued, so the
         // pass goes on fusing the next slice's gates
         if ((rc = r.eng->flush(r.pos + g < r.gates.size()))) { err = r.eng->err; return rc; }
+        if ((rc = cuda(cudaEventRecord(solo_ev_[k], es), "event")) ||
+            (rc = cuda(cudaStreamWaitEvent(stream_, solo_ev_[k], 0), "wait")))
+            return rc;
     }
     if ((rc = cuda(cudaEventRecord(ev2_, stream_), "event"))) return rc;
     in_flight_ = true;
@@ -377,7 +390,7 @@ int Server::retire(uint32_t* finished) {
     if (cudaEventElapsedTime(&ms, ev0_, ev1_) == cudaSuccess) busy_ms_ += ms;
     if (cudaEventElapsedTime(&ms_solo, ev1_, ev2_) == cudaSuccess) busy_ms_ += ms_solo;
     uint32_t fin = 0;
-    // solo circuits: measured rate, completion
+    // solo circuits: measured rate (of all of them together), completion
     uint64_t solo_gates = 0;
     for (uint64_t rid : solo_) solo_gates += reqs_.at(rid).chunk;
     std::vector<uint64_t> still;

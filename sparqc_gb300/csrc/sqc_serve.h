@@ -97,7 +97,7 @@ private:
         size_t bytes = 0;
     };
     std::vector<Spare> spare_;
-    static constexpr size_t kMaxSpare = 4;
+    static constexpr size_t kMaxSpare = 16;
     uint32_t inject_fail_ = 0;   // admissions left to fail on purpose (sqc_server_options.inject_alloc_failures)
     bool sched_ = false;         // circuits run in schedule_gates order
     // overlap_steps: a step leaves its slice in flight (in_flight_) and retires it at the next
@@ -143,6 +143,7 @@ private:
     size_t rcap_ = 0;
 
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, ev2_ = nullptr;
+    std::vector<cudaEvent_t> solo_ev_;   // end of each large circuit's part of a step
     uint64_t steps_ = 0, launches_ = 0, upd_done_ = 0;
     double busy_ms_ = 0.0;
 };
