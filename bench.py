@@ -57,7 +57,7 @@ def parse_args():
     ap.add_argument("--requests", type=int, default=300, help="c5: requests per arrival rate")
     ap.add_argument("--rates", type=str, default="50,1000", help="c5: arrival rates (circuits/s), comma-separated")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="c5: table memory budget")
-    ap.add_argument("--slice-ms", type=float, default=2.0, help="c5: serving time slice")
+    ap.add_argument("--slice-ms", type=float, default=1.0, help="c5: serving time slice")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--schedule", default="auto", choices=["auto", "on", "off"],
                     help="c4/c5: gates in sqc_schedule_gates order (auto: on in FP32, off in FP64)")
@@ -818,8 +818,8 @@ def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
     the same stream served in the given gate order beside it."""
     import torch
     reqs = circuits.serving_stream(requests, rate, seed=0)
-    lat0, makespan0, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0, schedule=False)
-    lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 2.0, schedule=True)
+    lat0, makespan0, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 1.0, schedule=False)
+    lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 1.0, schedule=True)
     lat, lat0 = np.array(lat), np.array(lat0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -831,7 +831,7 @@ def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
     plain_t = time.perf_counter() - t0
     served, served0, plain = len(reqs) / makespan, len(reqs) / makespan0, len(reqs) / plain_t
     return {"workload": f"c5: {requests} Poisson arrivals at {rate:g}/s of c4 circuits plus 5% large "
-                        "(48 qubits, k=24, 2000 gates), 120 GB budget, 2 ms slices, FP32, gates in scheduled order "
+                        "(48 qubits, k=24, 2000 gates), 120 GB budget, 1 ms slices, FP32, gates in scheduled order "
                         "(sqc_server_options.schedule_gates), overlapped steps (overlap_steps)",
             "circuits_per_s": served, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99)), "device_busy_s": st["busy_ms"] / 1e3,
