@@ -339,6 +339,17 @@ int Batch::grid() const {
 int Batch::run() {
     if (plans_.empty()) return fail(SQC_ERR_STATE, "no circuits prepared");
     int rc;
+    // every run restarts each circuit in a new epoch of its slice; before the 32-bit epoch could
+    // come back round to a value still stored in a header, the headers are cleared (the run
+    // restarts every circuit anyway) and the epoch starts over
+    if (++epoch_runs_ >= kBatchEpochRestart) {
+        for (const TableDev& t : tables_)
+            if ((rc = cuda(cudaMemsetAsync(t.hdr, 0, (t.mask + 1) * sizeof(Header), stream_), "cudaMemset(hdr)")))
+                return rc;
+        if ((rc = cuda(cudaMemsetAsync(&d_bctl_->epoch, 0, sizeof(d_bctl_->epoch), stream_), "cudaMemset(epoch)")))
+            return rc;
+        epoch_runs_ = 1;
+    }
     if ((rc = cuda(cudaEventRecord(ev0_, stream_), "event"))) return rc;
     if (use_graph_) {
         if (!graph_exec_) {

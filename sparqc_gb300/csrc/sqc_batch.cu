@@ -261,6 +261,7 @@ __global__ void batch_begin_kernel(BatchArgs a, unsigned long long deadline_ns) 
     __shared__ unsigned any_init;
     if (threadIdx.x == 0) {
         ep_new = a.bctl->epoch + 1;
+        if (ep_new == 0) ep_new = 1;   // epoch 0 marks cleared headers: never a live one
         running = 0;
         any_init = 0;
     }

@@ -135,6 +135,8 @@ private:
     bool ran_ = false, synced_ = false;
     double last_ms_ = 0.0;
     uint64_t launches_ = 0, runs_ = 0;
+    uint64_t epoch_runs_ = 0;   // runs since the slices' headers were last cleared
+    static constexpr uint64_t kBatchEpochRestart = 0xFFFFFF00ULL;
 };
 
 }  // namespace sqc

@@ -19,6 +19,7 @@ constexpr unsigned long long kMinBuckets = 64;
 constexpr size_t kFlushAt = 1024;          // queued gates that trigger a launch
 constexpr unsigned long long kTinyMaxList = 256;   // live buckets up to which a flush is one launch
 constexpr size_t kDescInitial = 1 << 14;   // descriptors held between verified syncs
+constexpr unsigned long long kEpochRestart = 0xFFFFFF00ULL;   // epochs before the headers are cleared
 constexpr double kMaxLoad = 0.9;           // live buckets a pair pass may leave behind
 
 unsigned long long pow2_at_least(unsigned long long x) {
@@ -231,9 +232,24 @@ int Engine::set_zero() {
     snap_log_ = 0;
     host_upd_ = 0;
     list_hint_ = 1;
-    int rc = cuda(launch_set_zero(dev(), ctl_, dbl_, stream_), "set_zero");
+    int rc;
+    if ((rc = next_epoch())) return rc;
+    rc = cuda(launch_set_zero(dev(), ctl_, dbl_, stream_), "set_zero");
     ++launches_;
     return rc;
+}
+
+// set_zero and set_state move the table to a new epoch (their kernels bump Ctl::epoch), and
+// headers of an older epoch read as empty. Before the 32-bit epoch could come back round to a
+// value still stored in a header, the headers are cleared and the epoch starts over.
+int Engine::next_epoch() {
+    if (++epochs_ < kEpochRestart) return SQC_OK;
+    epochs_ = 1;
+    int rc;
+    if ((rc = cuda(cudaMemsetAsync(tab_.hdr, 0, tab_.nb * sizeof(Header), stream_), "memset(headers)")) ||
+        (rc = cuda(cudaMemsetAsync(&ctl_->epoch, 0, sizeof(ctl_->epoch), stream_), "memset(epoch)")))
+        return rc;
+    return SQC_OK;
 }
 
 int Engine::set_state(const uint64_t* keys, const double* re, const double* im, uint64_t n,
@@ -291,6 +307,7 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
     snap_log_ = 0;
     host_upd_ = 0;
     list_hint_ = std::max<unsigned long long>(n, 1);
+    if ((rc = next_epoch())) return rc;
     rc = cuda(launch_set_state(d_rk_, d_rr_, d_ri_, n, dev(), ctl_, dbl_, sms_, stream_), "set_state");
     launches_ += n ? 5 : 2;
     if (rc) return rc;
@@ -611,7 +628,8 @@ int Engine::rebuild(unsigned long long nb_new) {
     if ((rc = alloc_table(nb_new, &nt))) return rc;
     const unsigned long long n_old = ctl_host_->list_n;
     Ctl c = *ctl_host_;
-    c.epoch = 1;
+    c.epoch = 1;   // a fresh table
+    epochs_ = 1;
     c.status = 0;
     c.done = 0;
     c.seq = 0;

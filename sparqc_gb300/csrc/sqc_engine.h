@@ -112,6 +112,8 @@ private:
     double thr_ = 1e-14;
     bool dev_upd_only_ = false;     // amp updates count device-applied gates only
     bool sched_ = false;            // each apply() call's gates go in schedule_gates order
+    unsigned long long epochs_ = 0; // epochs since the table's headers were last cleared
+    int next_epoch();
     std::vector<uint32_t> perm_;    // its scratch
     double lf_ = 0.5;
     uint32_t max_run_ = kMaxRun;
