@@ -169,6 +169,20 @@ int sqc_nnz(sqc_state* st, uint64_t* nnz);
 int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_t cap,
                   uint64_t* n, uint32_t flags);
 
+/* Asynchronous readout (no counterpart in the reference): as sqc_get_state without flags, into
+ * page-locked host arrays (cudaHostAlloc, cudaMallocHost or cudaHostRegister; *n too). The
+ * state's entries are gathered into a device buffer on the state's stream, and a copy on a
+ * stream of the state's own writes them to the host, so work queued on the state afterwards (a
+ * new circuit, more gates) runs while they travel. The arrays and *n hold the result once
+ * sqc_readout_wait returns, which returns SQC_ERR_CAPACITY if the state held more than cap
+ * entries (the first cap are written). The next sqc_get_state_async first completes the
+ * previous one as sqc_readout_wait does (returning its error); other readouts and
+ * sqc_set_state wait on the device for the copy before reusing the buffer. SQC_ERR_ARG for
+ * arrays that are not page-locked. */
+int sqc_get_state_async(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n);
+/* Wait for the state's asynchronous readout in flight, if any. */
+int sqc_readout_wait(sqc_state* st);
+
 /* Sum of |amplitude|^2, accumulated in FP64 on the device. */
 int sqc_norm2(sqc_state* st, double* norm2);
 

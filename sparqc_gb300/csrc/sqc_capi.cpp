@@ -117,6 +117,14 @@ int sqc_get_state(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_
     return guarded(st, [&](sqc::Engine& e) { return e.get_state(keys, re, im, cap, n, flags); });
 }
 
+int sqc_get_state_async(sqc_state* st, uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n) {
+    return guarded(st, [&](sqc::Engine& e) { return e.get_state_async(keys, re, im, cap, n); });
+}
+
+int sqc_readout_wait(sqc_state* st) {
+    return guarded(st, [&](sqc::Engine& e) { return e.readout_wait(); });
+}
+
 int sqc_norm2(sqc_state* st, double* norm2) {
     if (!norm2) return SQC_ERR_ARG;
     return guarded(st, [&](sqc::Engine& e) { return e.norm2(norm2); });

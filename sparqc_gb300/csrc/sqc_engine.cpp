@@ -33,6 +33,11 @@ unsigned long long pow2_at_least(unsigned long long x) {
 
 Engine::~Engine() {
     if (stream_) cudaStreamSynchronize(stream_);
+    if (copy_stream_) cudaStreamSynchronize(copy_stream_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
+    if (ev_gathered_) cudaEventDestroy(ev_gathered_);
+    if (ev_copied_) cudaEventDestroy(ev_copied_);
+    if (h_async_n_) cudaFreeHost(h_async_n_);
     free_table(&tab_);
     if (ctl_) cudaFree(ctl_);
     if (ctl_host_) cudaFreeHost(ctl_host_);
@@ -205,6 +210,10 @@ int Engine::ensure_desc(size_t n) {
 
 int Engine::ensure_readout(size_t n) {
     if (n <= rcap_) return SQC_OK;
+    if (async_pending_ && ev_copied_) {   // the buffers are about to be freed: the copy must be done
+        int rc;
+        if ((rc = cuda(cudaEventSynchronize(ev_copied_), "wait for the readout copy"))) return rc;
+    }
     const size_t cap = std::max<size_t>(n, 1024);
     if (d_rk_) cudaFree(d_rk_);
     if (d_rr_) cudaFree(d_rr_);
@@ -292,6 +301,7 @@ int Engine::set_state(const uint64_t* keys, const double* re, const double* im, 
         tab_ = nt;
     }
     if ((rc = ensure_readout(n))) return rc;
+    if ((rc = readout_buffers_free())) return rc;
     if (n) {
         if ((rc = cuda(cudaMemcpyAsync(d_rk_, keys, n * 8, cudaMemcpyHostToDevice, stream_), "H2D keys")) ||
             (rc = cuda(cudaMemcpyAsync(d_rr_, re, n * 8, cudaMemcpyHostToDevice, stream_), "H2D re")) ||
@@ -754,18 +764,85 @@ int Engine::ensure_sort(size_t n) {
     return SQC_OK;
 }
 
+// Work queued on the state's stream after this reuses the readout buffers only once the
+// asynchronous readout's copy (if one is in flight) has read them.
+int Engine::readout_buffers_free() {
+    if (!async_pending_) return SQC_OK;
+    return cuda(cudaStreamWaitEvent(stream_, ev_copied_, 0), "wait for the readout copy");
+}
+
+int Engine::get_state_async(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n) {
+    if (!n || (cap && (!keys || !re || !im))) return fail(SQC_ERR_ARG, "null argument");
+    // the copy engines write the arrays while the caller goes on: page-locked host memory only
+    void* host_ptr[4] = {keys, re, im, n};
+    for (int i = 0; i < 4; ++i) {
+        if (!host_ptr[i]) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, host_ptr[i]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            return fail(SQC_ERR_ARG, "asynchronous readout needs page-locked host arrays");
+        }
+    }
+    int rc;
+    // the queued gates go to the device first, so that they run while the previous
+    // asynchronous readout's copy finishes; that readout then completes
+    if ((rc = flush())) return rc;
+    if ((rc = readout_wait())) return rc;
+    if (!copy_stream_) {
+        if ((rc = cuda(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking), "cudaStreamCreate")) ||
+            (rc = cuda(cudaEventCreateWithFlags(&ev_gathered_, cudaEventDisableTiming), "event")) ||
+            (rc = cuda(cudaEventCreateWithFlags(&ev_copied_, cudaEventDisableTiming), "event")) ||
+            (rc = cuda(cudaMallocHost(&h_async_n_, sizeof(unsigned long long)), "cudaMallocHost")))
+            return rc;
+    }
+    unsigned long long got = 0;
+    if ((rc = readout_to_device(0, 0, false, &got, false))) return rc;   // gathered on the state's stream
+    // a whole-state readout gathers exactly the present keys: the synchronized count says how
+    // many bytes the copies move (the gathered count travels too and is checked on completion)
+    const unsigned long long expect = ctl_host_->nnz;
+    const unsigned long long m = std::min<unsigned long long>(expect, cap);
+    if ((rc = cuda(cudaEventRecord(ev_gathered_, stream_), "event")) ||
+        (rc = cuda(cudaStreamWaitEvent(copy_stream_, ev_gathered_, 0), "wait")) ||
+        (rc = cuda(cudaMemcpyAsync(h_async_n_, &ctl_->out_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                   copy_stream_), "D2H count")) ||
+        (rc = cuda(cudaMemcpyAsync(n, &ctl_->out_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                   copy_stream_), "D2H count")))
+        return rc;
+    if (m && ((rc = cuda(cudaMemcpyAsync(keys, d_rk_, m * 8, cudaMemcpyDeviceToHost, copy_stream_), "D2H keys")) ||
+              (rc = cuda(cudaMemcpyAsync(re, d_rr_, m * 8, cudaMemcpyDeviceToHost, copy_stream_), "D2H re")) ||
+              (rc = cuda(cudaMemcpyAsync(im, d_ri_, m * 8, cudaMemcpyDeviceToHost, copy_stream_), "D2H im"))))
+        return rc;
+    if ((rc = cuda(cudaEventRecord(ev_copied_, copy_stream_), "event"))) return rc;
+    async_cap_ = cap;
+    async_expect_ = expect;
+    async_pending_ = true;
+    return SQC_OK;
+}
+
+int Engine::readout_wait() {
+    if (!async_pending_) return SQC_OK;
+    int rc;
+    if ((rc = cuda(cudaEventSynchronize(ev_copied_), "wait for the readout copy"))) return rc;
+    async_pending_ = false;
+    if (*h_async_n_ != async_expect_) return fail(SQC_ERR_STATE, "asynchronous readout: entry count changed");
+    if (*h_async_n_ > async_cap_) return fail(SQC_ERR_CAPACITY, "output arrays too small");
+    return SQC_OK;
+}
+
 // Compact the present keys with (actual & mask) == value into the device readout arrays
 // (actual keys); *got receives their number (also when it exceeds the arrays).
-int Engine::readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got) {
+int Engine::readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got, bool wait) {
     int rc = sync();
     if (rc) return rc;
     if ((rc = ensure_readout(ctl_host_->nnz))) return rc;
+    if ((rc = readout_buffers_free())) return rc;
     if ((rc = cuda(cudaMemsetAsync(&ctl_->out_count, 0, sizeof(unsigned long long), stream_), "memset"))) return rc;
     if ((rc = cuda(launch_readout(dev(), ctl_, list_hint_, plan_.frame, dbl_, d_rk_, d_rr_, d_ri_, rcap_, drop_negl,
                                   prune_, sms_, stream_, mask, value ^ (plan_.frame & mask)),
                    "readout")))
         return rc;
     ++launches_;
+    if (!wait) return SQC_OK;
     if ((rc = read_ctl())) return rc;
     *got = ctl_host_->out_count;
     return SQC_OK;

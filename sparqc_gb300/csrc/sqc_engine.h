@@ -53,6 +53,13 @@ public:
     int sync();
     int nnz(uint64_t* out);
     int get_state(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n, uint32_t flags);
+    // Readout into page-locked host arrays that completes while later work on the state runs:
+    // the entries are gathered into the device readout buffers on the state's stream, then
+    // copies on a copy stream move them and the count to the host (sqc_get_state_async).
+    int get_state_async(uint64_t* keys, double* re, double* im, uint64_t cap, uint64_t* n);
+    // Wait for the asynchronous readout in flight (if any); SQC_ERR_CAPACITY if it held more
+    // entries than its arrays.
+    int readout_wait();
     // Readout of the keys with (key & mask) == value (actual keys, not the stored frame).
     int get_state_where(uint64_t mask, uint64_t value, uint64_t* keys, double* re, double* im, uint64_t cap,
                         uint64_t* n, uint32_t flags);
@@ -96,8 +103,10 @@ private:
     int repair(size_t failed_pass);
     int ensure_desc(size_t n);
     int ensure_readout(size_t n);
+    int readout_buffers_free();   // later users of the readout buffers wait for the async copy
     int ensure_sort(size_t n);
-    int readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got);
+    // wait = false: only queue the readout (the count stays on the device)
+    int readout_to_device(uint64_t mask, uint64_t value, bool drop_negl, unsigned long long* got, bool wait = true);
     bool plan_gate(const sqc_gate& g, GateDesc* out);
     int read_ctl();
     int read_sums();   // copy the exact sums back and wait
@@ -112,6 +121,12 @@ private:
     double thr_ = 1e-14;
     bool dev_upd_only_ = false;     // amp updates count device-applied gates only
     bool sched_ = false;            // each apply() call's gates go in schedule_gates order
+    // asynchronous readout: copy stream, gathered / copied events, count word
+    cudaStream_t copy_stream_ = nullptr;
+    cudaEvent_t ev_gathered_ = nullptr, ev_copied_ = nullptr;
+    unsigned long long* h_async_n_ = nullptr;   // page-locked: the gathered count, once copied
+    uint64_t async_cap_ = 0, async_expect_ = 0;
+    bool async_pending_ = false;
     unsigned long long epochs_ = 0; // epochs since the table's headers were last cleared
     int next_epoch();
     std::vector<uint32_t> perm_;    // its scratch

@@ -24,6 +24,7 @@ EXPORTS = ("sqc_default_options", "sqc_create", "sqc_destroy", "sqc_set_zero_sta
            "sqc_status_string", "sqc_last_error", "sqc_stream", "sqc_apply_fixed",
            "sqc_get_state_where", "sqc_probability", "sqc_measure", "sqc_sample", "sqc_swap", "sqc_save",
            "sqc_load", "sqc_fp64_rate", "sqc_twoq_gates", "sqc_apply_twoq", "sqc_schedule_gates",
+           "sqc_get_state_async", "sqc_readout_wait",
            "sqc_batch_default_options", "sqc_batch_create", "sqc_batch_destroy", "sqc_batch_prepare",
            "sqc_batch_run", "sqc_batch_sync", "sqc_batch_circuit_status", "sqc_batch_nnz", "sqc_batch_get_state",
            "sqc_batch_get_states",
@@ -377,6 +378,16 @@ class State:
                     "get_state")
         m = got.value
         return keys[:m].copy(), re[:m].copy(), im[:m].copy()
+
+    def state_async(self, keys, re, im, count):
+        """Start an asynchronous readout into page-locked arrays (keys uint64, re/im float64 of
+        equal size, count a one-element uint64 array, all page-locked); readout_wait() completes it
+        and the entry count is then count[0]."""
+        self._check(self._L.sqc_get_state_async(self._h, _p(keys), _p(re), _p(im), keys.size, _p(count)),
+                    "get_state_async")
+
+    def readout_wait(self):
+        self._check(self._L.sqc_readout_wait(self._h), "readout_wait")
 
     def state_where(self, mask, value, sorted=True, drop_negligible=False):
         """Entries whose keys have (key & mask) == value."""

@@ -3,7 +3,7 @@
 With equal precision the engine and the oracle execute the same roundings, so states are
 compared bit for bit (keys, real and imaginary parts). Against the golden fixtures (made on
 another machine's libm) and the dense statevector the tolerance is 1e-12 relative with a
-1e-14 absolute floor (the prune threshold). FP32 states are judged by fidelity >= 1 - 1e-6
+1e-14 absolute floor (the prune threshold). FP32 states are checked by fidelity >= 1 - 1e-6
 against FP64.
 """
 import os
