@@ -123,6 +123,7 @@ int Server::init(const sqc_server_options* opt) {
     std::memset(h_limit_, 0, n * sizeof(unsigned));
     alloc_.reset(budget);
     slot_req_.assign(n, 0);
+    in_rid_.assign(n, 0);
     free_slots_.resize(n);
     for (size_t i = 0; i < n; ++i) free_slots_[i] = (int)(n - 1 - i);   // back() is the lowest slot
     return SQC_OK;
@@ -312,15 +313,25 @@ int Server::step(uint32_t* finished) {
     if (finished) *finished = 0;
     int rc;
     uint32_t fin = 0;
-    if (in_flight_ && (rc = retire(&fin))) return rc;   // the previous step's slice (overlap_steps)
-    if (finished) *finished = fin;
-    if ((rc = admit())) return rc;
+    if (in_flight_) {
+        // overlap_steps: the previous step's slice is still running. Admission (planning done,
+        // engines made, slices cleared and uploaded) is host work and stream-ordered device
+        // work, so it goes first; then the slice is retired. Retiring frees no memory, so
+        // nothing more could be admitted after it.
+        if ((rc = admit())) return rc;
+        if ((rc = retire(&fin))) return rc;
+        if (finished) *finished = fin;
+    } else if ((rc = admit())) {
+        return rc;
+    }
     bool any = false;
     for (uint32_t s = 0; s < n_used_ && !any; ++s)
         any = slot_req_[s] && reqs_.at(slot_req_[s]).state == SQC_REQ_RUNNING;
     if (!any && solo_.empty()) return cuda(cudaStreamSynchronize(stream_), "sync");
     const uint32_t n = n_used_;
     if ((rc = cuda(cudaEventRecord(ev0_, stream_), "event"))) return rc;
+    for (uint32_t s = 0; s < n; ++s)   // the requests this launch runs, for its retirement
+        in_rid_[s] = slot_req_[s] && reqs_.at(slot_req_[s]).state == SQC_REQ_RUNNING ? slot_req_[s] : 0;
     if (any) {
         // the small circuits: one time slice of the persistent kernel over the resident slots
         std::memcpy(stg_circ_, h_circ_, n * sizeof(BCirc));
@@ -423,9 +434,8 @@ int Server::retire(uint32_t* finished) {
     const bool timeout = any && h_bctl_->status == ST_TIMEOUT;
     for (uint32_t s = 0; any && s < n; ++s) {
         const uint64_t rid = slot_req_[s];
-        if (!rid) continue;
+        if (!rid || rid != in_rid_[s]) continue;   // not run by this launch (free, done, or admitted since)
         Request& r = reqs_.at(rid);
-        if (r.state != SQC_REQ_RUNNING) { h_cmd_[s] = BC_KEEP; continue; }
         const unsigned st = h_sched_[s].state;
         if (st == BS_PARKED && !timeout) {
             h_cmd_[s] = BC_RESUME;

@@ -130,6 +130,7 @@ private:
     BatchCtl* h_bctl_ = nullptr;
 
     std::vector<uint64_t> slot_req_;     // request id per slot, 0 = free
+    std::vector<uint64_t> in_rid_;       // running request per slot when the slice in flight launched
     std::vector<int> free_slots_;
     uint32_t n_used_ = 0;                // slots [0, n_used_) are scanned by the kernel
     std::deque<uint64_t> queue_;
