@@ -846,7 +846,11 @@ def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
     import torch
     reqs = circuits.serving_stream(requests, rate, seed=0)
     lat0, makespan0, _ = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 1.0, schedule=False)
-    lat, makespan, st = serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 1.0, schedule=True)
+    # the served stream's throughput varies from run to run (how many large circuits overlap
+    # depends on how arrivals fall between steps): three runs, the median one reported
+    runs = sorted((serve_stream(engine, stream.cuda_stream, reqs, 32, 120e9, 1.0, schedule=True) for _ in range(3)),
+                  key=lambda x: x[1])
+    lat, makespan, st = runs[1]
     lat, lat0 = np.array(lat), np.array(lat0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -862,7 +866,8 @@ def serve_summary(engine, circuits, stream, requests=300, rate=1000.0):
                         "(sqc_server_options.schedule_gates), overlapped steps (overlap_steps)",
             "circuits_per_s": served, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99)), "device_busy_s": st["busy_ms"] / 1e3,
-            "makespan_s": makespan,
+            "makespan_s": makespan, "runs_circuits_per_s": [len(reqs) / r[1] for r in runs],
+            "reported": "median of 3 runs",
             "plain_fp64_circuits_per_s": plain, "speedup_vs_plain_fp64": served / plain,
             "large": int(sum(1 for r in reqs if r[2] == 24)),
             "given_order": {"circuits_per_s": served0, "p50_ms": 1e3 * float(np.percentile(lat0, 50)),
