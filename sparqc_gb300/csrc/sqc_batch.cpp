@@ -175,7 +175,7 @@ int Batch::prepare(const sqc_circuit_desc* cs, uint32_t n) {
         if (cs[i].n_gates && !cs[i].gates) return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": null gates");
         nqs[i] = cs[i].nq;
         gates[i].assign(cs[i].gates, cs[i].gates + cs[i].n_gates);
-        if (sched_ && cs[i].n_gates > 1) {   // schedule_gates order for quad passes, whatever the tuning
+        if (sched_ && cs[i].n_gates > 1 && cs[i].n_gates <= kScheduleMaxGates) {   // schedule_gates order for quads, whatever the tuning
             for (uint64_t j = 0; j < cs[i].n_gates; ++j)
                 if (const char* why = check_gate(cs[i].gates[j], cs[i].nq))
                     return fail(SQC_ERR_ARG, "circuit " + std::to_string(i) + ": " + why);

@@ -199,7 +199,7 @@ int sqc_twoq_gates(uint32_t form, uint32_t a, uint32_t b, uint32_t c, uint64_t c
 
 int sqc_schedule_gates(uint32_t nq, const sqc_gate* gates, uint64_t n, uint32_t max_cross_qubits, uint32_t* perm) {
     if (nq < 1 || nq > 64 || max_cross_qubits < 1 || max_cross_qubits > 3 || (n && (!gates || !perm)) ||
-        n > 0xFFFFFFFFULL)
+        n > sqc::kScheduleMaxGates)
         return SQC_ERR_ARG;
     for (uint64_t i = 0; i < n; ++i)
         if (sqc::check_gate(gates[i], nq)) return SQC_ERR_ARG;

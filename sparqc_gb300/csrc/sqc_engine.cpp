@@ -337,7 +337,7 @@ int Engine::apply(const sqc_gate* gates, uint64_t n) {
     for (uint64_t i = 0; i < n; ++i) {
         if (const char* why = check_gate(gates[i], nq_)) return fail(SQC_ERR_ARG, why);
     }
-    if (sched_ && n > 1) {   // the call's gates in the order passes fuse better (sqc_schedule_gates)
+    if (sched_ && n > 1 && n <= kScheduleMaxGates) {   // the call's gates in the order passes fuse better
         perm_.resize(n);
         schedule_gates(gates, n, max_nx_, max_run_, kScheduleWindow, perm_.data());
         for (uint64_t i = 0; i < n; ++i) pending_.push_back(gates[perm_[i]]);

@@ -92,6 +92,8 @@ void schedule_gates(const sqc_gate* g, size_t n, uint32_t max_nx, size_t max_run
 constexpr uint32_t kSchedCandidates = 6;
 constexpr uint32_t kSchedTrialWindow = 64;   // gates the candidate choices are compared over
 constexpr size_t kScheduleWindow = 256;
+// Longer gate arrays (indices no longer fit 32 bits) keep the order given.
+constexpr uint64_t kScheduleMaxGates = 0xFFFFFFFFULL;
 
 // Largest number of 16-key groups a state can ever hold while running a gate sequence whose
 // planning ended in p (starting from keys that agreed on every bit of the starting kmask):

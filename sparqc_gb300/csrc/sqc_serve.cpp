@@ -144,7 +144,7 @@ int Server::submit(const sqc_circuit_desc* c, uint64_t* id) {
     // (three cross-group qubits in FP32, two in FP64) or the pool's quads. The group bound, and
     // so the placement just decided, does not depend on the order.
     std::vector<sqc_gate> sched;
-    if (sched_ && c->n_gates > 1) {
+    if (sched_ && c->n_gates > 1 && c->n_gates <= kScheduleMaxGates) {
         std::vector<uint32_t> perm(c->n_gates);
         schedule_gates(c->gates, c->n_gates, r.solo && !dbl_ ? 3u : 2u, kMaxRun, kScheduleWindow, perm.data());
         sched.resize(c->n_gates);
