@@ -576,7 +576,8 @@ def run_gpu(args):
                            "another order, so not bit-identical to the reference; the headline keeps the given order"}
 
     extras = {}
-    if not args.no_extras and world == 1 and args.workload == "c3" and args.k is None and args.gates is None:
+    if (not args.no_extras and world == 1 and args.workload == "c3" and args.k is None and args.gates is None
+            and args.precision == 64):
         from sparqc_gb300 import circuits as circ
         extras["c1"] = single_summary(engine, "c1", stream, args.steps, flush)
         extras["c2"] = single_summary(engine, "c2", stream, args.steps, flush)
