@@ -275,8 +275,8 @@ constexpr int kResolveThreads = 256;
 template <int NX>
 __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
     constexpr int K = 1 << NX;
-    __shared__ unsigned warp_at[kResolveThreads / 32];
-    __shared__ unsigned long long base_sh;
+    __shared__ unsigned warp_at[2][kResolveThreads / 32];   // two sets: chunk parity
+    __shared__ unsigned long long base_sh[2];
     Ctl* ctl = a.ctl;
     if (*(volatile unsigned int*)&ctl->status) return;
     const unsigned long long n = ctl->list_n;
@@ -293,8 +293,9 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
     };
     const TableDev t = a.t;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int par = 0;
     for (unsigned long long c0 = (unsigned long long)blockIdx.x * kResolveThreads; c0 < n;
-         c0 += (unsigned long long)gridDim.x * kResolveThreads) {
+         c0 += (unsigned long long)gridDim.x * kResolveThreads, par ^= 1) {
         const unsigned long long e = c0 + threadIdx.x;
         bool own = false;
         unsigned b = kNoBucket;
@@ -309,19 +310,19 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
             for (int k = 0; k < idx && own; ++k) own = lookup_group(t, ep, member(G0, k)) < 0;
         }
         const unsigned bal = __ballot_sync(kFull, own);
-        if (lane == 0) warp_at[w] = __popc(bal);
+        if (lane == 0) warp_at[par][w] = __popc(bal);
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned tot = 0;
             for (int i = 0; i < kResolveThreads / 32; ++i) {
-                const unsigned c = warp_at[i];
-                warp_at[i] = tot;
+                const unsigned c = warp_at[par][i];
+                warp_at[par][i] = tot;
                 tot += c;
             }
-            base_sh = tot ? atomicAdd(&ctl->units_n, (unsigned long long)tot) : 0ULL;
+            base_sh[par] = tot ? atomicAdd(&ctl->units_n, (unsigned long long)tot) : 0ULL;
         }
         __syncthreads();
-        const unsigned long long pos = base_sh + warp_at[w] + __popc(bal & ((1u << lane) - 1u));
+        const unsigned long long pos = base_sh[par] + warp_at[par][w] + __popc(bal & ((1u << lane) - 1u));
         // members of this warp's owners, 32 / K owners per round, lane r * K + k on member k
         unsigned rem = bal;
         while (rem) {
@@ -345,7 +346,10 @@ __global__ void __launch_bounds__(kResolveThreads) resolve_kernel(PassArgs a) {
                 if (k == 0) u->G0 = sG0;
             }
         }
-        __syncthreads();   // warp_at and base_sh are reused by the next chunk
+        // the next chunk uses the other set of warp_at / base_sh, and the chunk after it writes
+        // this set again only past the next chunk's barriers, which no warp passes before it
+        // has read this set (one barrier fewer per chunk than a barrier here: FP64 64-qubit
+        // workload 74.09 -> 73.68 ms, FP32 28.23 -> 28.11 ms)
     }
 }
 
