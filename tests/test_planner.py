@@ -148,6 +148,62 @@ int main() {
         const uint32_t wk[6] = {1, 2, 3, 4, 5, 0};
         for (int i = 0; i < 6; ++i) CHECK(pk[i] == wk[i]);
     }
+    // every gate plans the same in the scheduled order as in the given one (same resolution on
+    // the host, same descriptor), and the planner ends in the same state: random circuits of
+    // every gate kind, up to three controls, on 12, 40 and 64 qubits
+    {
+        unsigned long long rs = 0x9E3779B97F4A7C15ULL;
+        auto rnd = [&]() { rs = rs * 6364136223846793005ULL + 1442695040888963407ULL; return rs >> 33; };
+        const uint32_t kinds[] = {KX, KY, KZ, KH, KPHASE, KRZ, KRX, KRY, KS, KSDG, KT, KTDG, KU};
+        int checked = 0, moved = 0;
+        for (uint32_t nq : {12u, 40u, 64u}) {
+            for (int rep = 0; rep < 4; ++rep) {
+                std::vector<sqc_gate> gs;
+                const uint32_t kq = nq < 16 ? nq : 16;   // branching gates stay below qubit kq
+                for (uint32_t q = 0; q < kq; ++q) gs.push_back(g(KH, q));
+                for (int i = 0; i < 400; ++i) {
+                    const uint32_t kind = kinds[rnd() % 13];
+                    const bool branch = kind == KH || kind == KRX || kind == KRY || kind == KU;
+                    const uint32_t t = (uint32_t)(branch ? rnd() % kq : rnd() % nq);
+                    uint64_t ctl = 0;
+                    for (uint32_t c = 0, nc = (uint32_t)(rnd() % 4); c < nc; ++c) {
+                        const uint32_t q = (uint32_t)(rnd() % nq);
+                        if (q != t) ctl |= 1ULL << q;
+                    }
+                    sqc_gate x = g(kind, t, ctl, 0.1 + 0.01 * (double)(rnd() % 500));
+                    x.phi = 0.3; x.lambda = 0.7;
+                    gs.push_back(x);
+                }
+                for (uint32_t mx = 1; mx <= 3; ++mx) {
+                    std::vector<uint32_t> perm(gs.size());
+                    schedule_gates(gs.data(), gs.size(), mx, 64, 256, perm.data());
+                    std::vector<char> seen(gs.size(), 0);
+                    bool ok = true;
+                    for (uint32_t i : perm) { ok = ok && i < gs.size() && !seen[i]; if (i < gs.size()) seen[i] = 1; }
+                    CHECK(ok);
+                    if (!ok) continue;
+                    Planner a, b;
+                    std::vector<GateDesc> da(gs.size()), db(gs.size());
+                    std::vector<char> ra(gs.size()), rb(gs.size());
+                    for (size_t i = 0; i < gs.size(); ++i) { std::memset(&da[i], 0, sizeof(GateDesc)); ra[i] = plan_gate(a, gs[i], &da[i]); }
+                    for (size_t j = 0; j < gs.size(); ++j) {
+                        const uint32_t i = perm[j];
+                        std::memset(&db[i], 0, sizeof(GateDesc));
+                        rb[i] = plan_gate(b, gs[i], &db[i]);
+                        moved += i != j;
+                    }
+                    for (size_t i = 0; i < gs.size(); ++i) {
+                        da[i].pad = db[i].pad = 0;   // the credit of host-resolved gates before it
+                        CHECK(ra[i] == rb[i]);
+                        CHECK(!ra[i] || std::memcmp(&da[i], &db[i], sizeof(GateDesc)) == 0);
+                        ++checked;
+                    }
+                    CHECK(a.frame == b.frame && a.kmask == b.kmask && a.kval == b.kval);
+                }
+            }
+        }
+        CHECK(checked > 10000 && moved > 1000);
+    }
 
     std::printf("fails=%d\n", fails);
     return fails ? 1 : 0;

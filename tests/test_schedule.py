@@ -97,6 +97,19 @@ def test_schedule_keeps_the_state():
         assert np.max(np.abs(a.psi - b.psi)) < 1e-12
 
 
+def test_schedule_keeps_the_state_with_two_qubit_gates():
+    # U gates with controls and the relabelling X gates of two-qubit sequences
+    from test_twoq import mixed_circuit
+    for seed in range(3):
+        g, _, _ = mixed_circuit(10, 8, seed)
+        a = DenseOracle(10)
+        a.apply(g)
+        for mx in (1, 2, 3):
+            b = DenseOracle(10)
+            b.apply(g[schedule_gates(10, g, mx)])
+            assert np.max(np.abs(a.psi - b.psi)) < 1e-12
+
+
 def test_schedule_bad_arguments():
     g = G.gate_array([(G.H, 3), (G.H, 5)])
     with pytest.raises(SparqcError):
