@@ -450,7 +450,7 @@ def run_gpu(args):
     got = engine.ctypes.c_uint64()
     L = engine.load()
     gates_c = np.ascontiguousarray(gates)
-    e2e_steps = max(3, min(args.steps, 5))
+    e2e_steps = max(3, min(args.steps, 10))
     read_s = [0.0]
 
     def e2e_step_sync():
